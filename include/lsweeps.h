@@ -1,0 +1,187 @@
+/*
+ * lsweeps.h -- C ABI of the GB300 L-sweeps library (liblsweeps_gb300.so).
+ *
+ * The library solves the 2D Helmholtz equation  -Lap u - omega^2 m(x) u = f
+ * (5-point finite differences, cubic PML) with GMRES preconditioned by the
+ * checkerboard L-sweep domain-decomposition preconditioner, on one GB300 GPU.
+ * It replaces the hot path of the reference (paths relative to its root):
+ *   DDCheckerboard            src/DDCheckerboard.cpp, include/DD.h:14-114
+ *   SubdomainStructured       src/SubdomainStructured.cpp, include/Subdomain.h:20-227
+ *   LocalLinearSolver         include/LocalLinearSolver.h:8-41 (EigenSparseLU ->
+ *                             batched block-tridiagonal factorisation on the GPU)
+ *   GlobalIterativeSolverGMRES src/GlobalIterativeSolverGMRES.cpp:65-348
+ *   AssemblerHelmholtz2DFD / PMLCubic2D  src/AssemblerHelmholtz2DFD.cpp:371-457,
+ *                             src/PMLCubic2D.cpp:35-236
+ *
+ * Conventions
+ *   - The domain is [0, n_g h]^2 with n_g = N m + N - 1 elements per side
+ *     (DDCheckerboard.cpp:119); the global DOF grid has n_dof = n_g + 2p - 1
+ *     nodes per side (PML included), node G at coordinate (G + 1 - p) h.
+ *   - Global vectors are complex128, interleaved (re, im), x-major with y
+ *     fastest: index = Gx * n_dof + Gy (the reference's DOF order,
+ *     AssemblerHelmholtz2DFD.cpp:166-177, applied globally).  A batch of nrhs
+ *     vectors is stored back to back.
+ *   - Pointers named *_dev are device pointers owned by the caller; *_host are
+ *     host pointers.  `stream` is a cudaStream_t (NULL = legacy default stream).
+ *   - Every call returns an lsw_status instead of exiting the process (the
+ *     reference prints to cerr and calls exit(1)).  One context per host thread,
+ *     or external locking; the library keeps no global state except the
+ *     library-wide status strings.
+ */
+#ifndef LSWEEPS_H
+#define LSWEEPS_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum lsw_status {
+  LSW_OK = 0,
+  LSW_ERR_INVALID_ARGUMENT = 1,
+  LSW_ERR_CUDA = 2,
+  LSW_ERR_OUT_OF_MEMORY = 3,
+  LSW_ERR_NOT_SET_UP = 4,
+  LSW_ERR_NOT_FACTORIZED = 5,
+  LSW_ERR_SINGULAR_BLOCK = 6,
+  LSW_ERR_NOT_CONVERGED = 7,
+  LSW_ERR_UNSUPPORTED = 8
+} lsw_status;
+
+/* Arithmetic of the subdomain factors and preconditioner applies.  The DD
+ * matvec, Krylov vectors, Arnoldi and Hessenberg work are always FP64. */
+typedef enum lsw_precision {
+  LSW_PREC_C128 = 0, /* complex double factors and applies (reference arithmetic) */
+  LSW_PREC_C64 = 1   /* complex float factors and applies, FP32 accumulation */
+} lsw_precision;
+
+typedef enum lsw_gmres_mode {
+  /* GlobalIterativeSolverGMRES::solve as written: left preconditioning, no
+   * restart, x0 = M^-1 b, conjugate-first MGS dot, the reference's Givens
+   * bookkeeping and a square solve of H (GlobalIterativeSolverGMRES.cpp:65-348).
+   * Its logged residual is the parity quantity; it is not a true residual. */
+  LSW_GMRES_REFERENCE = 0,
+  /* Right-preconditioned flexible GMRES(restart), MGS, complex Givens; stops on
+   * the true FP64 residual ||b - A x|| / ||b|| <= tol. */
+  LSW_GMRES_FLEXIBLE = 1
+} lsw_gmres_mode;
+
+typedef struct lsw_ctx lsw_ctx;
+
+/* DDCheckerboard::setUp arguments (DDCheckerboard.cpp:87-94) restricted to the
+ * square case NCellsX == NCellsY, NX == NY, with the PML given in cells. */
+typedef struct lsw_geom {
+  int n_cells;       /* cells per side, N >= 1 */
+  int n_els_in_cell; /* interior elements per cell side, m > 4 (DDCheckerboard.cpp:106-111) */
+  int pml;           /* PML thickness in cells, p >= 1 */
+  int order;         /* finite-difference order; only 2 (5-point) is supported */
+  double h;          /* mesh size */
+} lsw_geom;
+
+typedef struct lsw_problem_info {
+  int n_g;            /* elements per side of the physical domain */
+  int n_dof;          /* DOFs per side of the global grid (PML included) */
+  int n_cells_total;  /* N * N */
+  int max_cell_side;  /* largest cell DOF count per side */
+  int precision;      /* lsw_precision */
+  int factorized;     /* 1 after lsw_factorize */
+  long long factor_bytes;  /* bytes of the resident subdomain factors */
+  long long device_bytes;  /* all device memory held by the problem */
+  double omega;
+  double pml_C;       /* PML absorption C = ln(omega) (Input.cpp:836) */
+} lsw_problem_info;
+
+/* One subdomain (SubdomainStructured) in local DOF coordinates:
+ * local DOF (i, j) <-> global DOF (lo_x + i, lo_y + j). */
+typedef struct lsw_cell_info {
+  int I, J;            /* cell row (y) and column (x) */
+  int nx, ny;          /* DOFs per side of the cell (x-lines, points per line) */
+  int lo_x, lo_y;      /* global DOF index of local DOF 0 */
+  int lines_x[2][4];   /* local x of trace0, trace1, traceN, traceNP; [0] non-shifted,
+                          [1] shifted; -1 where the cell has no such trace */
+  int lines_y[2][4];
+  int own_x[2][2];     /* owned local range [lo, hi] along x (mValsToKeep*) */
+  int own_y[2][2];
+} lsw_cell_info;
+
+typedef struct lsw_gmres_opts {
+  int mode;        /* lsw_gmres_mode */
+  double tol;      /* relative tolerance (reference default 1e-6) */
+  int max_iter;    /* iteration cap (reference default 40) */
+  int restart;     /* FGMRES restart length; ignored in reference mode */
+  int verbose;     /* print the residual log to stdout */
+} lsw_gmres_opts;
+
+typedef struct lsw_gmres_report {
+  int iterations;      /* iterations taken (max over the right-hand sides) */
+  int converged;       /* 1 if every right-hand side met tol */
+  double final_log;    /* last logged relative residual (max over rhs) */
+  double true_rel_res; /* ||b - A x|| / ||b|| after the solve, FP64, max over rhs */
+  double seconds;      /* wall time of the solve */
+  int precond_applies; /* preconditioner applications (per right-hand side batch) */
+  double* log;         /* optional caller buffer for the residual log of rhs 0 */
+  int log_capacity;
+  int log_len;
+} lsw_gmres_report;
+
+/* ---- context ------------------------------------------------------------- */
+lsw_status lsw_ctx_create(lsw_ctx** ctx, int device);
+lsw_status lsw_ctx_destroy(lsw_ctx* ctx);
+const char* lsw_status_string(lsw_status s);
+const char* lsw_ctx_last_error(const lsw_ctx* ctx);
+
+/* Geometry of cell `cell` (index I*N + J) of a decomposition, computed on the
+ * host without a GPU (DDCheckerboard::setUp trace limits, DDCheckerboard.cpp:214-419,
+ * and SubdomainStructured::assignIndexSets, SubdomainStructured.cpp:1019-1116). */
+lsw_status lsw_geometry_cell(const lsw_geom* geom, int cell, lsw_cell_info* out);
+
+/* ---- problem ------------------------------------------------------------- */
+/* DDCheckerboard::setUp (DDCheckerboard.cpp:87-645) + the assembler set-up of
+ * Input::readAssemblerHelmholtz2DFD (Input.cpp:795-857): builds the cells,
+ * trace geometry, sweep schedules and the device-resident operator.
+ * m_grid_host: squared slowness on the n_dof x n_dof global grid (x-major). */
+lsw_status lsw_problem_setup(lsw_ctx* ctx, const lsw_geom* geom, const double* m_grid_host,
+                             double omega, int precision);
+lsw_status lsw_problem_info_get(const lsw_ctx* ctx, lsw_problem_info* out);
+lsw_status lsw_cell_info_get(const lsw_ctx* ctx, int cell, lsw_cell_info* out);
+
+/* DDCheckerboard::factorize (DDCheckerboard.cpp:648-665) ->
+ * LocalLinearSolverEigenSparseLU::factorize (LocalLinearSolverEigenSparseLU.cpp:40-62):
+ * every cell factorised in one batched launch; idempotent. */
+lsw_status lsw_factorize(lsw_ctx* ctx, void* stream);
+
+/* DDCheckerboard::applyPrecond (DDCheckerboard.cpp:687-739): y = M^-1 x for a
+ * batch of nrhs global vectors. */
+lsw_status lsw_apply_precond(lsw_ctx* ctx, const void* x_dev, void* y_dev, int nrhs, void* stream);
+
+/* DDCheckerboard::applySystemMatrix (DDCheckerboard.cpp:2611-2635): y = A x,
+ * the global 5-point operator, FP64. */
+lsw_status lsw_apply_A(lsw_ctx* ctx, const void* x_dev, void* y_dev, int nrhs, void* stream);
+
+/* DDCheckerboard::assembleRHS (DDCheckerboard.cpp:668-684) with RHSSrcPts
+ * (RHSSrcPts.cpp:87-112): Gaussian point sources of width = DD mesh size.
+ * src_xy_host: nsrc (x, y) pairs; amp_host: nsrc amplitudes or NULL (= 1).
+ * Writes one global vector. */
+lsw_status lsw_assemble_rhs(lsw_ctx* ctx, const double* src_xy_host, const double* amp_host,
+                            int nsrc, void* b_dev, void* stream);
+
+/* GlobalIterativeSolverGMRES::solve (GlobalIterativeSolverGMRES.cpp:65-203)
+ * on device vectors; every right-hand side of the batch is iterated in
+ * lockstep and shares each preconditioner launch. */
+lsw_status lsw_gmres(lsw_ctx* ctx, const void* b_dev, void* x_dev, int nrhs,
+                     const lsw_gmres_opts* opts, lsw_gmres_report* report, void* stream);
+
+/* GlobalIterativeSolver::solve(rhs, res) (include/GlobalIterativeSolver.h:48)
+ * on host buffers: copies b to the device, solves, copies x back. */
+lsw_status lsw_solve_host(lsw_ctx* ctx, const double* b_host, double* x_host, int nrhs,
+                          const lsw_gmres_opts* opts, lsw_gmres_report* report, void* stream);
+
+/* LocalLinearSolver::solve (include/LocalLinearSolver.h:40) for one cell:
+ * x = A_cell^-1 b on full cell vectors (nx*ny complex128, local order i*ny+j),
+ * nrhs vectors back to back. */
+lsw_status lsw_local_solve(lsw_ctx* ctx, int cell, const void* b_dev, void* x_dev, int nrhs,
+                           void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LSWEEPS_H */

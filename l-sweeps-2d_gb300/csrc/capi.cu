@@ -1,0 +1,833 @@
+// C ABI of the GB300 L-sweeps library (declared in include/lsweeps.h).
+#include "common.cuh"
+#include "internal.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <stdexcept>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace lsw {
+bool factor_needs_work(int max_ny, bool dbl);
+int front_rmax(bool dbl);
+}
+
+using namespace lsw;
+using cplx = std::complex<double>;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  ~DevBuf() { if (p) cudaFree(p); }
+  cudaError_t ensure(size_t b) {
+    if (b <= bytes && p) return cudaSuccess;
+    if (p) { cudaFree(p); p = nullptr; bytes = 0; }
+    if (b == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess) bytes = b;
+    return e;
+  }
+  template <typename X> X* as() const { return reinterpret_cast<X*>(p); }
+};
+
+struct lsw_ctx {
+  int device = 0;
+  std::string err;
+  // problem
+  bool is_setup = false, factorized = false;
+  lsw_geom geom{};
+  int N = 0, m = 0, p = 0, n_g = 0, n_dof = 0, prec = 0;
+  double h = 0, omega = 0, C = 0;
+  long long n2 = 0;
+  int max_nx = 0, max_ny = 0, ncell = 0;
+  long long LP = 0;
+  std::vector<DevCell> cells;
+  DevBuf d_cells, d_prof, d_gprof, d_m, d_fac, d_work, d_status;
+  // per batch size
+  std::map<int, std::unique_ptr<Schedule>> sched;
+  std::map<int, std::unique_ptr<DevBuf[]>> sched_bufs;
+  DevBuf d_traces, d_outs, d_scratch;
+  // Krylov workspace
+  DevBuf k_basis, k_zbasis, k_tmp, k_tmp2, k_r, k_part, k_small, k_small2, k_nrm;
+  // local-solve workspace
+  DevBuf ls_items, ls_slots, ls_scratch;
+  size_t fixed_bytes = 0;
+};
+
+namespace {
+
+const char* kStatusStr[] = {"LSW_OK", "LSW_ERR_INVALID_ARGUMENT", "LSW_ERR_CUDA", "LSW_ERR_OUT_OF_MEMORY",
+                            "LSW_ERR_NOT_SET_UP", "LSW_ERR_NOT_FACTORIZED", "LSW_ERR_SINGULAR_BLOCK",
+                            "LSW_ERR_NOT_CONVERGED", "LSW_ERR_UNSUPPORTED"};
+
+lsw_status fail(lsw_ctx* c, lsw_status s, const std::string& msg) {
+  if (c) c->err = msg;
+  return s;
+}
+lsw_status cuda_fail(lsw_ctx* c, cudaError_t e, const char* where) {
+  std::string msg = std::string(where) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return fail(c, LSW_ERR_OUT_OF_MEMORY, msg);
+  return fail(c, LSW_ERR_CUDA, msg);
+}
+#define CK(call, where)                                     \
+  do {                                                      \
+    cudaError_t _e = (call);                                \
+    if (_e != cudaSuccess) return cuda_fail(ctx, _e, where); \
+  } while (0)
+
+inline size_t csize(int prec) { return prec == LSW_PREC_C64 ? 8 : 16; }
+inline cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+DevCell make_cell(int I, int J, int N, int m, int p) {
+  DevCell c{};
+  const DirGeom gx = dir_geom(J, N, m, p), gy = dir_geom(I, N, m, p);
+  c.I = I; c.J = J;
+  c.nx = gx.nd; c.ny = gy.nd;
+  c.lox = gx.lo; c.loy = gy.lo;
+  c.ldn = (gy.nd + 3) & ~3;
+  for (int s = 0; s < 2; ++s) {
+    for (int l = 0; l < 4; ++l) { c.lx[s][l] = gx.lines[s][l]; c.ly[s][l] = gy.lines[s][l]; }
+    c.ownx[s][0] = gx.own[s][0]; c.ownx[s][1] = gx.own[s][1];
+    c.owny[s][0] = gy.own[s][0]; c.owny[s][1] = gy.own[s][1];
+  }
+  return c;
+}
+
+void fill_info(const DevCell& c, lsw_cell_info* o) {
+  o->I = c.I; o->J = c.J; o->nx = c.nx; o->ny = c.ny; o->lo_x = c.lox; o->lo_y = c.loy;
+  for (int s = 0; s < 2; ++s) {
+    for (int l = 0; l < 4; ++l) { o->lines_x[s][l] = c.lx[s][l]; o->lines_y[s][l] = c.ly[s][l]; }
+    o->own_x[s][0] = c.ownx[s][0]; o->own_x[s][1] = c.ownx[s][1];
+    o->own_y[s][0] = c.owny[s][0]; o->own_y[s][1] = c.owny[s][1];
+  }
+}
+
+void push_profile(std::vector<double2>& v, const Profile1D& pr) {
+  const size_t n = pr.lo_re.size();
+  for (size_t i = 0; i < n; ++i) v.push_back(make_double2(pr.lo_re[i], pr.lo_im[i]));
+  for (size_t i = 0; i < n; ++i) v.push_back(make_double2(pr.hi_re[i], pr.hi_im[i]));
+  for (size_t i = 0; i < n; ++i) v.push_back(make_double2(pr.dg_re[i], pr.dg_im[i]));
+}
+
+size_t device_bytes(const lsw_ctx* c) {
+  size_t b = c->d_cells.bytes + c->d_prof.bytes + c->d_gprof.bytes + c->d_m.bytes + c->d_fac.bytes +
+             c->d_work.bytes + c->d_status.bytes + c->d_traces.bytes + c->d_outs.bytes + c->d_scratch.bytes +
+             c->k_basis.bytes + c->k_zbasis.bytes + c->k_tmp.bytes + c->k_tmp2.bytes + c->k_r.bytes +
+             c->k_part.bytes + c->k_small.bytes + c->k_small2.bytes + c->k_nrm.bytes + c->ls_items.bytes +
+             c->ls_slots.bytes + c->ls_scratch.bytes;
+  for (auto& kv : c->sched_bufs)
+    for (int i = 0; i < 3; ++i) b += kv.second[i].bytes;
+  return b;
+}
+
+lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out) {
+  auto it = ctx->sched.find(nrhs);
+  const bool dbl = ctx->prec == LSW_PREC_C128;
+  if (it == ctx->sched.end()) {
+    std::unique_ptr<Schedule> sc(new Schedule);
+    std::vector<DevItem> items; std::vector<DevSlot> slots; std::vector<DevGroup> groups;
+    try {
+      build_schedule(ctx->cells, ctx->N, nrhs, front_rmax(dbl), ctx->LP, sc->fronts, items, slots, groups, ctx->n2);
+    } catch (const std::exception& ex) {
+      return fail(ctx, LSW_ERR_UNSUPPORTED, ex.what());
+    }
+    sc->nrhs = nrhs;
+    for (auto& f : sc->fronts) sc->scratch_elems = std::max(sc->scratch_elems, f.scratch_elems);
+    std::unique_ptr<DevBuf[]> bufs(new DevBuf[3]);
+    CK(bufs[0].ensure(std::max<size_t>(1, items.size()) * sizeof(DevItem)), "cudaMalloc(items)");
+    CK(bufs[1].ensure(std::max<size_t>(1, slots.size()) * sizeof(DevSlot)), "cudaMalloc(slots)");
+    CK(bufs[2].ensure(std::max<size_t>(1, groups.size()) * sizeof(DevGroup)), "cudaMalloc(groups)");
+    CK(cudaMemcpy(bufs[0].p, items.data(), items.size() * sizeof(DevItem), cudaMemcpyHostToDevice), "H2D items");
+    CK(cudaMemcpy(bufs[1].p, slots.data(), slots.size() * sizeof(DevSlot), cudaMemcpyHostToDevice), "H2D slots");
+    CK(cudaMemcpy(bufs[2].p, groups.data(), groups.size() * sizeof(DevGroup), cudaMemcpyHostToDevice), "H2D groups");
+    sc->d_items = bufs[0].as<DevItem>();
+    sc->d_slots = bufs[1].as<DevSlot>();
+    sc->d_groups = bufs[2].as<DevGroup>();
+    ctx->sched_bufs[nrhs] = std::move(bufs);
+    it = ctx->sched.emplace(nrhs, std::move(sc)).first;
+  }
+  Schedule* sc = it->second.get();
+  const size_t cs = csize(ctx->prec);
+  CK(ctx->d_traces.ensure((size_t)nrhs * 4 * ctx->ncell * 24 * ctx->LP * cs), "cudaMalloc(traces)");
+  CK(ctx->d_outs.ensure((size_t)nrhs * 4 * ctx->n2 * cs), "cudaMalloc(outs)");
+  CK(ctx->d_scratch.ensure(std::max<size_t>(1, (size_t)sc->scratch_elems * cs)), "cudaMalloc(scratch)");
+  *out = sc;
+  return LSW_OK;
+}
+
+lsw_status precond_impl(lsw_ctx* ctx, const double2* x, double2* y, int nrhs, cudaStream_t st) {
+  Schedule* sc = nullptr;
+  lsw_status s = ensure_batch(ctx, nrhs, &sc);
+  if (s != LSW_OK) return s;
+  const size_t cs = csize(ctx->prec);
+  CK(cudaMemsetAsync(ctx->d_traces.p, 0, (size_t)nrhs * 4 * ctx->ncell * 24 * ctx->LP * cs, st), "memset traces");
+  CK(cudaMemsetAsync(ctx->d_outs.p, 0, (size_t)nrhs * 4 * ctx->n2 * cs, st), "memset outs");
+  FrontArgs a{};
+  a.cells = ctx->d_cells.as<DevCell>();
+  a.slots = sc->d_slots;
+  a.groups = sc->d_groups;
+  a.fac = ctx->d_fac.p;
+  a.prof = ctx->d_prof.as<double2>();
+  a.traces = ctx->d_traces.p;
+  a.outs = ctx->d_outs.p;
+  a.scratch = ctx->d_scratch.p;
+  a.x_in = x;
+  a.x_stride = ctx->n2;
+  a.n_dof = ctx->n_dof; a.N = ctx->N; a.m = ctx->m; a.p = ctx->p;
+  for (const Front& f : sc->fronts) {
+    a.items = sc->d_items + f.item_begin;
+    a.item_count = f.item_count;
+    cudaError_t e = ctx->prec == LSW_PREC_C64 ? launch_front<float>(a, ctx->max_ny, st)
+                                              : launch_front<double>(a, ctx->max_ny, st);
+    CK(e, "front kernel");
+  }
+  cudaError_t e = ctx->prec == LSW_PREC_C64 ? launch_combine<float>(ctx->d_outs.p, y, nrhs, ctx->n2, st)
+                                            : launch_combine<double>(ctx->d_outs.p, y, nrhs, ctx->n2, st);
+  CK(e, "combine kernel");
+  return LSW_OK;
+}
+
+lsw_status apply_A_impl(lsw_ctx* ctx, const double2* x, double2* y, int nrhs, cudaStream_t st) {
+  CK(launch_apply_A(x, y, nrhs, ctx->n_dof, ctx->d_gprof.as<double2>(), ctx->d_m.as<double>(),
+                    ctx->omega * ctx->omega, st), "apply_A kernel");
+  return LSW_OK;
+}
+
+// complex Gaussian elimination with partial pivoting, square system (host)
+std::vector<cplx> dense_solve(std::vector<cplx> A, std::vector<cplx> b, int n) {
+  std::vector<int> perm(n);
+  for (int i = 0; i < n; ++i) perm[i] = i;
+  for (int k = 0; k < n; ++k) {
+    int pr = k; double best = std::abs(A[k * n + k]);
+    for (int i = k + 1; i < n; ++i) if (std::abs(A[i * n + k]) > best) { best = std::abs(A[i * n + k]); pr = i; }
+    if (pr != k) { for (int j = 0; j < n; ++j) std::swap(A[k * n + j], A[pr * n + j]); std::swap(b[k], b[pr]); }
+    if (A[k * n + k] == cplx(0, 0)) continue;
+    for (int i = k + 1; i < n; ++i) {
+      const cplx f = A[i * n + k] / A[k * n + k];
+      if (f == cplx(0, 0)) continue;
+      for (int j = k; j < n; ++j) A[i * n + j] -= f * A[k * n + j];
+      b[i] -= f * b[k];
+    }
+  }
+  std::vector<cplx> x(n);
+  for (int i = n - 1; i >= 0; --i) {
+    cplx s = b[i];
+    for (int j = i + 1; j < n; ++j) s -= A[i * n + j] * x[j];
+    x[i] = A[i * n + i] == cplx(0, 0) ? cplx(0, 0) : s / A[i * n + i];
+  }
+  return x;
+}
+
+// givens_rotation (GlobalIterativeSolverGMRES.cpp:333-348), kept as written
+void givens_ref(cplx v1, cplx v2, cplx& cs, cplx& sn) {
+  if (v1 == cplx(0.0, 0.0)) { cs = 0.0; sn = 1.0; return; }
+  const cplx t = std::pow(std::pow(v1, 2.0) + std::pow(v2, 2.0), 0.5);
+  cs = std::abs(v1) / t;
+  sn = cs * v2 / v1;
+}
+
+struct Krylov {
+  lsw_ctx* ctx;
+  cudaStream_t st;
+  int nv;
+  long long n2;
+  lsw_status st_ = LSW_OK;
+  double2* part() { return ctx->k_part.as<double2>(); }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* lsw_status_string(lsw_status s) {
+  const int i = (int)s;
+  if (i < 0 || i > 8) return "LSW_UNKNOWN";
+  return kStatusStr[i];
+}
+
+const char* lsw_ctx_last_error(const lsw_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+lsw_status lsw_ctx_create(lsw_ctx** out, int device) {
+  if (!out) return LSW_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return LSW_ERR_CUDA;
+  if (device < 0 || device >= n) return LSW_ERR_INVALID_ARGUMENT;
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return LSW_ERR_CUDA;
+  lsw_ctx* c = new lsw_ctx;
+  c->device = device;
+  *out = c;
+  return LSW_OK;
+}
+
+lsw_status lsw_ctx_destroy(lsw_ctx* ctx) {
+  if (!ctx) return LSW_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(ctx->device);
+  delete ctx;
+  return LSW_OK;
+}
+
+lsw_status lsw_geometry_cell(const lsw_geom* g, int cell, lsw_cell_info* out) {
+  std::string why;
+  if (!out || !geom_valid(g, &why)) return LSW_ERR_INVALID_ARGUMENT;
+  const int N = g->n_cells;
+  if (cell < 0 || cell >= N * N) return LSW_ERR_INVALID_ARGUMENT;
+  fill_info(make_cell(cell / N, cell % N, N, g->n_els_in_cell, g->pml), out);
+  return LSW_OK;
+}
+
+lsw_status lsw_problem_setup(lsw_ctx* ctx, const lsw_geom* g, const double* m_grid, double omega, int precision) {
+  if (!ctx) return LSW_ERR_INVALID_ARGUMENT;
+  std::string why;
+  if (!geom_valid(g, &why)) return fail(ctx, LSW_ERR_INVALID_ARGUMENT, why);
+  if (!m_grid) return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "m_grid is NULL");
+  if (!(omega > 1.0) || !std::isfinite(omega))
+    return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "omega must be > 1 (PML absorption C = ln omega must be positive)");
+  if (precision != LSW_PREC_C128 && precision != LSW_PREC_C64)
+    return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "unknown precision");
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  // drop everything of a previous problem
+  ctx->sched.clear(); ctx->sched_bufs.clear();
+  ctx->is_setup = false; ctx->factorized = false;
+  ctx->geom = *g;
+  ctx->N = g->n_cells; ctx->m = g->n_els_in_cell; ctx->p = g->pml; ctx->h = g->h;
+  ctx->n_g = ctx->N * ctx->m + ctx->N - 1;
+  ctx->n_dof = ctx->n_g + 2 * ctx->p - 1;
+  ctx->n2 = (long long)ctx->n_dof * ctx->n_dof;
+  ctx->omega = omega;
+  ctx->C = std::log(omega);   // Input.cpp:836
+  ctx->prec = precision;
+  ctx->ncell = ctx->N * ctx->N;
+  ctx->cells.clear();
+  std::vector<double2> prof;
+  long long fac_off = 0;
+  ctx->max_nx = ctx->max_ny = 0;
+  for (int I = 0; I < ctx->N; ++I)
+    for (int J = 0; J < ctx->N; ++J) {
+      DevCell c = make_cell(I, J, ctx->N, ctx->m, ctx->p);
+      c.fac_off = fac_off;
+      fac_off += (long long)c.nx * c.ny * c.ldn;
+      c.prof_off = (long long)prof.size();
+      const DirGeom gx = dir_geom(J, ctx->N, ctx->m, ctx->p), gy = dir_geom(I, ctx->N, ctx->m, ctx->p);
+      push_profile(prof, make_profile(gx.nel, ctx->p, ctx->h, ctx->C));
+      push_profile(prof, make_profile(gy.nel, ctx->p, ctx->h, ctx->C));
+      ctx->max_nx = std::max(ctx->max_nx, c.nx);
+      ctx->max_ny = std::max(ctx->max_ny, c.ny);
+      ctx->cells.push_back(c);
+    }
+  ctx->LP = ((std::max(ctx->max_nx, ctx->max_ny) + 7) / 8) * 8;
+  std::vector<double2> gprof;
+  push_profile(gprof, make_profile(ctx->n_g, ctx->p, ctx->h, ctx->C));
+  const size_t cs = csize(precision);
+  CK(ctx->d_cells.ensure(ctx->cells.size() * sizeof(DevCell)), "cudaMalloc(cells)");
+  CK(ctx->d_prof.ensure(prof.size() * sizeof(double2)), "cudaMalloc(prof)");
+  CK(ctx->d_gprof.ensure(gprof.size() * sizeof(double2)), "cudaMalloc(gprof)");
+  CK(ctx->d_m.ensure((size_t)ctx->n2 * sizeof(double)), "cudaMalloc(m)");
+  CK(ctx->d_fac.ensure((size_t)fac_off * cs), "cudaMalloc(factors)");
+  CK(ctx->d_status.ensure(16), "cudaMalloc(status)");
+  const bool dbl = precision == LSW_PREC_C128;
+  if (factor_needs_work(ctx->max_ny, dbl)) {
+    CK(ctx->d_work.ensure((size_t)ctx->ncell * ctx->max_ny * ctx->max_ny * cs), "cudaMalloc(factor work)");
+  }
+  CK(cudaMemcpy(ctx->d_cells.p, ctx->cells.data(), ctx->cells.size() * sizeof(DevCell), cudaMemcpyHostToDevice), "H2D cells");
+  CK(cudaMemcpy(ctx->d_prof.p, prof.data(), prof.size() * sizeof(double2), cudaMemcpyHostToDevice), "H2D prof");
+  CK(cudaMemcpy(ctx->d_gprof.p, gprof.data(), gprof.size() * sizeof(double2), cudaMemcpyHostToDevice), "H2D gprof");
+  CK(cudaMemcpy(ctx->d_m.p, m_grid, (size_t)ctx->n2 * sizeof(double), cudaMemcpyHostToDevice), "H2D m");
+  ctx->is_setup = true;
+  return LSW_OK;
+}
+
+lsw_status lsw_problem_info_get(const lsw_ctx* ctx, lsw_problem_info* o) {
+  if (!ctx || !o) return LSW_ERR_INVALID_ARGUMENT;
+  if (!ctx->is_setup) return LSW_ERR_NOT_SET_UP;
+  o->n_g = ctx->n_g; o->n_dof = ctx->n_dof; o->n_cells_total = ctx->ncell;
+  o->max_cell_side = std::max(ctx->max_nx, ctx->max_ny);
+  o->precision = ctx->prec; o->factorized = ctx->factorized ? 1 : 0;
+  o->factor_bytes = (long long)ctx->d_fac.bytes;
+  o->device_bytes = (long long)device_bytes(ctx);
+  o->omega = ctx->omega; o->pml_C = ctx->C;
+  return LSW_OK;
+}
+
+lsw_status lsw_cell_info_get(const lsw_ctx* ctx, int cell, lsw_cell_info* o) {
+  if (!ctx || !o) return LSW_ERR_INVALID_ARGUMENT;
+  if (!ctx->is_setup) return LSW_ERR_NOT_SET_UP;
+  if (cell < 0 || cell >= ctx->ncell) return LSW_ERR_INVALID_ARGUMENT;
+  fill_info(ctx->cells[cell], o);
+  return LSW_OK;
+}
+
+lsw_status lsw_factorize(lsw_ctx* ctx, void* stream) {
+  if (!ctx) return LSW_ERR_INVALID_ARGUMENT;
+  if (!ctx->is_setup) return fail(ctx, LSW_ERR_NOT_SET_UP, "lsw_problem_setup first");
+  if (ctx->factorized) return LSW_OK;   // idempotent (LocalLinearSolverEigenSparseLU.cpp:42-45)
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  cudaStream_t st = S(stream);
+  CK(cudaMemsetAsync(ctx->d_status.p, 0, 16, st), "memset status");
+  const double w2 = ctx->omega * ctx->omega;
+  cudaError_t e = ctx->prec == LSW_PREC_C64
+                      ? launch_factorize<float>(ctx->d_cells.as<DevCell>(), ctx->ncell, ctx->d_prof.as<double2>(),
+                                                ctx->d_m.as<double>(), ctx->n_dof, w2, ctx->d_fac.p, ctx->d_work.p,
+                                                ctx->max_ny, ctx->d_status.as<int>(), st)
+                      : launch_factorize<double>(ctx->d_cells.as<DevCell>(), ctx->ncell, ctx->d_prof.as<double2>(),
+                                                 ctx->d_m.as<double>(), ctx->n_dof, w2, ctx->d_fac.p, ctx->d_work.p,
+                                                 ctx->max_ny, ctx->d_status.as<int>(), st);
+  CK(e, "factorize kernel");
+  int status = 0;
+  CK(cudaMemcpyAsync(&status, ctx->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H status");
+  CK(cudaStreamSynchronize(st), "factorize sync");
+  if (status & 1) return fail(ctx, LSW_ERR_SINGULAR_BLOCK, "zero or non-finite pivot in a Schur complement block");
+  ctx->factorized = true;
+  return LSW_OK;
+}
+
+lsw_status lsw_apply_precond(lsw_ctx* ctx, const void* x, void* y, int nrhs, void* stream) {
+  if (!ctx || !x || !y || nrhs < 1) return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "bad arguments to lsw_apply_precond");
+  if (!ctx->is_setup) return fail(ctx, LSW_ERR_NOT_SET_UP, "lsw_problem_setup first");
+  if (!ctx->factorized) return fail(ctx, LSW_ERR_NOT_FACTORIZED, "lsw_factorize first");
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  return precond_impl(ctx, reinterpret_cast<const double2*>(x), reinterpret_cast<double2*>(y), nrhs, S(stream));
+}
+
+lsw_status lsw_apply_A(lsw_ctx* ctx, const void* x, void* y, int nrhs, void* stream) {
+  if (!ctx || !x || !y || nrhs < 1) return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "bad arguments to lsw_apply_A");
+  if (!ctx->is_setup) return fail(ctx, LSW_ERR_NOT_SET_UP, "lsw_problem_setup first");
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  return apply_A_impl(ctx, reinterpret_cast<const double2*>(x), reinterpret_cast<double2*>(y), nrhs, S(stream));
+}
+
+lsw_status lsw_assemble_rhs(lsw_ctx* ctx, const double* src, const double* amp, int nsrc, void* b, void* stream) {
+  if (!ctx || !b || nsrc < 0 || (nsrc > 0 && !src)) return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "bad arguments to lsw_assemble_rhs");
+  if (!ctx->is_setup) return fail(ctx, LSW_ERR_NOT_SET_UP, "lsw_problem_setup first");
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  cudaStream_t st = S(stream);
+  std::vector<double> hs(2 * std::max(nsrc, 1) + std::max(nsrc, 1));
+  for (int i = 0; i < 2 * nsrc; ++i) hs[i] = src[i];
+  for (int i = 0; i < nsrc; ++i) hs[2 * nsrc + i] = amp ? amp[i] : 1.0;
+  CK(ctx->k_small2.ensure(hs.size() * sizeof(double) + 64), "cudaMalloc(src)");
+  CK(cudaMemcpyAsync(ctx->k_small2.p, hs.data(), hs.size() * sizeof(double), cudaMemcpyHostToDevice, st), "H2D src");
+  // eps = DD mesh size (Input.cpp:243): every cell has mesh size h on the integer grid
+  CK(launch_rhs(reinterpret_cast<double2*>(b), ctx->n_dof, ctx->p, ctx->h, ctx->k_small2.as<double>(),
+                ctx->k_small2.as<double>() + 2 * nsrc, nsrc, ctx->h, st), "rhs kernel");
+  CK(cudaStreamSynchronize(st), "rhs sync");
+  return LSW_OK;
+}
+
+lsw_status lsw_local_solve(lsw_ctx* ctx, int cell, const void* b, void* x, int nrhs, void* stream) {
+  if (!ctx || !b || !x || nrhs < 1) return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "bad arguments to lsw_local_solve");
+  if (!ctx->is_setup) return fail(ctx, LSW_ERR_NOT_SET_UP, "lsw_problem_setup first");
+  if (cell < 0 || cell >= ctx->ncell) return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "cell index out of range");
+  if (!ctx->factorized)   // LocalLinearSolverEigenSparseLU.cpp:68-72
+    return fail(ctx, LSW_ERR_NOT_FACTORIZED, "The linear system has to be factorized before it can be solved");
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  cudaStream_t st = S(stream);
+  const bool dbl = ctx->prec == LSW_PREC_C128;
+  const int rmax = front_rmax(dbl);
+  const DevCell& cl = ctx->cells[cell];
+  std::vector<DevItem> items;
+  std::vector<DevSlot> slots;
+  long long scr = 0;
+  for (int r0 = 0; r0 < nrhs; r0 += rmax) {
+    DevItem it{};
+    it.cell = cell; it.slot_begin = (int)slots.size(); it.group_begin = 0; it.group_count = 0;
+    it.slot_count = std::min(rmax, nrhs - r0);
+    it.scratch_off = scr;
+    scr += (long long)cl.nx * it.slot_count * cl.ldn;
+    for (int r = r0; r < r0 + it.slot_count; ++r) {
+      DevSlot s{};
+      s.kind = SK_CELLVEC; s.rhs = r;
+      s.in_lr0 = s.in_lr1 = s.in_ud0 = s.in_ud1 = -1;
+      slots.push_back(s);
+    }
+    items.push_back(it);
+  }
+  CK(ctx->ls_items.ensure(items.size() * sizeof(DevItem)), "cudaMalloc(ls items)");
+  CK(ctx->ls_slots.ensure(slots.size() * sizeof(DevSlot)), "cudaMalloc(ls slots)");
+  CK(ctx->ls_scratch.ensure((size_t)scr * csize(ctx->prec)), "cudaMalloc(ls scratch)");
+  CK(cudaMemcpyAsync(ctx->ls_items.p, items.data(), items.size() * sizeof(DevItem), cudaMemcpyHostToDevice, st), "H2D");
+  CK(cudaMemcpyAsync(ctx->ls_slots.p, slots.data(), slots.size() * sizeof(DevSlot), cudaMemcpyHostToDevice, st), "H2D");
+  FrontArgs a{};
+  a.cells = ctx->d_cells.as<DevCell>();
+  a.items = ctx->ls_items.as<DevItem>();
+  a.slots = ctx->ls_slots.as<DevSlot>();
+  a.groups = nullptr;
+  a.fac = ctx->d_fac.p;
+  a.prof = ctx->d_prof.as<double2>();
+  a.traces = nullptr; a.outs = nullptr;
+  a.scratch = ctx->ls_scratch.p;
+  a.x_in = reinterpret_cast<const double2*>(b);
+  a.x_stride = (long long)cl.nx * cl.ny;
+  a.x_out = reinterpret_cast<double2*>(x);
+  a.out_stride = (long long)cl.nx * cl.ny;
+  a.n_dof = ctx->n_dof; a.N = ctx->N; a.m = ctx->m; a.p = ctx->p;
+  a.item_count = (int)items.size();
+  cudaError_t e = dbl ? launch_front<double>(a, ctx->max_ny, st) : launch_front<float>(a, ctx->max_ny, st);
+  CK(e, "local solve kernel");
+  CK(cudaStreamSynchronize(st), "local solve sync");
+  return LSW_OK;
+}
+
+// ---------------------------------------------------------------------------
+// GMRES
+// ---------------------------------------------------------------------------
+static lsw_status gmres_reference(lsw_ctx* ctx, const double2* b, double2* x, int nv, const lsw_gmres_opts* o,
+                                  lsw_gmres_report* rep, cudaStream_t st) {
+  const long long n2 = ctx->n2;
+  const size_t vb = (size_t)nv * n2 * sizeof(double2);
+  const int maxit = o->max_iter;
+  CK(ctx->k_basis.ensure(vb * (size_t)(maxit + 1)), "cudaMalloc(Q)");
+  CK(ctx->k_tmp.ensure(vb), "cudaMalloc(tmp)");
+  CK(ctx->k_r.ensure(vb), "cudaMalloc(rhsPrec)");
+  CK(ctx->k_part.ensure((size_t)nv * 1216 * sizeof(double2)), "cudaMalloc(partials)");
+  CK(ctx->k_small.ensure((size_t)nv * (maxit + 2) * sizeof(double2) + 64), "cudaMalloc(h)");
+  CK(ctx->k_small2.ensure((size_t)nv * (maxit + 2) * sizeof(double2) + 64), "cudaMalloc(coef)");
+  CK(ctx->k_nrm.ensure((size_t)nv * 2 * sizeof(double2) + 64), "cudaMalloc(nrm)");
+  double2* Q = ctx->k_basis.as<double2>();
+  double2* tmp = ctx->k_tmp.as<double2>();
+  double2* rp = ctx->k_r.as<double2>();
+  double2* part = ctx->k_part.as<double2>();
+  double2* hdev = ctx->k_small.as<double2>();
+  double2* cdev = ctx->k_small2.as<double2>();
+  double* ndev = ctx->k_nrm.as<double>();
+  auto Qi = [&](int i) { return Q + (size_t)i * nv * n2; };
+  lsw_status s;
+  int applies = 0;
+  // rhsPrec = M^-1 b ; x0 = rhsPrec (GlobalIterativeSolverGMRES.cpp:75-78)
+  if ((s = precond_impl(ctx, b, rp, nv, st)) != LSW_OK) return s;
+  ++applies;
+  CK(cudaMemcpyAsync(x, rp, vb, cudaMemcpyDeviceToDevice, st), "copy x0");
+  // r = rhsPrec - M^-1 A x0 (81-84), stored as Q_0 before normalisation
+  if ((s = apply_A_impl(ctx, x, tmp, nv, st)) != LSW_OK) return s;
+  if ((s = precond_impl(ctx, tmp, Qi(0), nv, st)) != LSW_OK) return s;
+  ++applies;
+  for (int v = 0; v < nv; ++v) CK(launch_sub(Qi(0) + v * n2, rp + v * n2, Qi(0) + v * n2, n2, st), "sub");
+  CK(launch_norm2(rp, n2, nv, n2, reinterpret_cast<double*>(part), ndev, st), "norm");
+  CK(launch_norm2(Qi(0), n2, nv, n2, reinterpret_cast<double*>(part), ndev + nv, st), "norm");
+  std::vector<double> hn(2 * nv);
+  CK(cudaMemcpyAsync(hn.data(), ndev, 2 * nv * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H norms");
+  CK(cudaStreamSynchronize(st), "sync");
+  std::vector<double> rhs_norm(nv), r_norm(nv);
+  std::vector<std::vector<double>> logs(nv);
+  std::vector<int> done(nv, 0), lastk(nv, -1);
+  for (int v = 0; v < nv; ++v) {
+    rhs_norm[v] = std::sqrt(hn[v]);
+    r_norm[v] = std::sqrt(hn[nv + v]);
+    logs[v].push_back(r_norm[v] / rhs_norm[v]);
+    if (logs[v][0] < o->tol || maxit == 0) done[v] = 1;   // (115-116)
+  }
+  if (o->verbose) printf("iteration 0: %.6e\n", logs[0][0]);
+  bool all = std::all_of(done.begin(), done.end(), [](int d) { return d != 0; });
+  std::vector<std::vector<cplx>> H(nv), beta(nv), cs(nv), sn(nv);
+  int kmax = -1;
+  if (!all) {
+    std::vector<double2> rsc(nv);
+    for (int v = 0; v < nv; ++v) rsc[v] = make_double2(r_norm[v], 0.0);
+    CK(cudaMemcpyAsync(cdev, rsc.data(), nv * sizeof(double2), cudaMemcpyHostToDevice, st), "H2D");
+    CK(launch_scale(Qi(0), Qi(0), cdev, 1, n2, nv, n2, st), "scale");
+    for (int v = 0; v < nv; ++v) beta[v].push_back(cplx(r_norm[v], 0.0));
+    for (int k = 0; k < maxit; ++k) {
+      // arnoldi (238-310): q = M^-1 A Q_k ; h_i = q.dot(Q_i) = sum conj(q) Q_i ; q -= h_i Q_i
+      if ((s = apply_A_impl(ctx, Qi(k), tmp, nv, st)) != LSW_OK) return s;
+      double2* q = Qi(k + 1);
+      if ((s = precond_impl(ctx, tmp, q, nv, st)) != LSW_OK) return s;
+      ++applies;
+      CK(launch_dot(q, Qi(0), n2, nv, n2, part, hdev, st), "dot");
+      for (int i = 0; i <= k; ++i) {
+        // coefficients for all rhs of column i sit at hdev[i*nv + v]
+        if (i < k)
+          CK(launch_axpy_dot(q, Qi(i), hdev + (size_t)i * nv, Qi(i + 1), n2, nv, n2, part,
+                             hdev + (size_t)(i + 1) * nv, 1, st), "axpy_dot");
+        else
+          CK(launch_axpy_dot(q, Qi(i), hdev + (size_t)i * nv, nullptr, n2, nv, n2, part,
+                             hdev + (size_t)(k + 1) * nv, 1, st), "axpy_norm");
+      }
+      std::vector<double2> hh((size_t)(k + 2) * nv);
+      CK(cudaMemcpyAsync(hh.data(), hdev, hh.size() * sizeof(double2), cudaMemcpyDeviceToHost, st), "D2H h");
+      CK(cudaStreamSynchronize(st), "sync");
+      std::vector<double2> sc(nv);
+      for (int v = 0; v < nv; ++v) {
+        std::vector<cplx> h(k + 2);
+        for (int i = 0; i <= k; ++i) h[i] = cplx(hh[(size_t)i * nv + v].x, hh[(size_t)i * nv + v].y);
+        const double qn = std::sqrt(hh[(size_t)(k + 1) * nv + v].x);
+        h[k + 1] = qn;
+        sc[v] = make_double2(qn != 0.0 ? qn : 1.0, 0.0);
+        // apply_givens_rotation (313-330): rotations 0..k-2 only
+        for (int i = 1; i < k; ++i) {
+          const cplx t = cs[v][i - 1] * h[i - 1] + sn[v][i - 1] * h[i];
+          h[i] = -sn[v][i - 1] * h[i - 1] + cs[v][i - 1] * h[i];
+          h[i - 1] = t;
+        }
+        cplx c_, s_;
+        givens_ref(h[k], h[k + 1], c_, s_);
+        h[k] = c_ * h[k] + s_ * h[k + 1];
+        h[k + 1] = 0.0;
+        cs[v].push_back(c_); sn[v].push_back(s_);
+        // H grows by one row and one column (134-162)
+        std::vector<cplx> Hn((size_t)(k + 2) * (k + 1), cplx(0, 0));
+        for (int i = 0; i < k + 1; ++i)
+          for (int j = 0; j < k; ++j) Hn[(size_t)i * (k + 1) + j] = H[v][(size_t)i * k + j];
+        for (int i = 0; i < k + 2; ++i) Hn[(size_t)i * (k + 1) + k] = h[i];
+        H[v].swap(Hn);
+        beta[v].push_back(-sn[v][k] * beta[v][k]);   // (168-171)
+        beta[v][k] *= cs[v][k];
+        if (!done[v]) {
+          logs[v].push_back(std::abs(beta[v].back()) / rhs_norm[v]);
+          if (logs[v].back() <= o->tol || k == maxit - 1) { done[v] = 1; lastk[v] = k; }
+        }
+      }
+      if (o->verbose) printf("iteration %d: %.6e\n", k + 1, logs[0].back());
+      CK(cudaMemcpyAsync(cdev, sc.data(), nv * sizeof(double2), cudaMemcpyHostToDevice, st), "H2D");
+      CK(launch_scale(q, q, cdev, 1, n2, nv, n2, st), "scale");
+      kmax = k;
+      if (std::all_of(done.begin(), done.end(), [](int d) { return d != 0; })) break;
+    }
+    // y = H(0:k,0:k)^-1 beta ; x += Q y  (194-201)
+    const int ncol = kmax + 1;
+    std::vector<double2> coef((size_t)nv * ncol, make_double2(0, 0));
+    for (int v = 0; v < nv; ++v) {
+      if (lastk[v] < 0) continue;
+      const int kk = lastk[v] + 1;
+      std::vector<cplx> A((size_t)kk * kk), rhs(kk);
+      const int cols = kmax + 1;
+      for (int i = 0; i < kk; ++i) {
+        rhs[i] = beta[v][i];
+        for (int j = 0; j < kk; ++j) A[(size_t)i * kk + j] = H[v][(size_t)i * cols + j];
+      }
+      std::vector<cplx> y = dense_solve(A, rhs, kk);
+      for (int i = 0; i < kk; ++i) coef[(size_t)v * ncol + i] = make_double2(y[i].real(), y[i].imag());
+    }
+    CK(ctx->k_small2.ensure(coef.size() * sizeof(double2) + 64), "cudaMalloc(coef)");
+    cdev = ctx->k_small2.as<double2>();
+    CK(cudaMemcpyAsync(cdev, coef.data(), coef.size() * sizeof(double2), cudaMemcpyHostToDevice, st), "H2D y");
+    CK(launch_lincomb(x, Q, (long long)nv * n2, n2, cdev, ncol, n2, nv, n2, st), "lincomb");
+  }
+  int iters = 0;
+  double fl = 0.0;
+  for (int v = 0; v < nv; ++v) {
+    iters = std::max(iters, (int)logs[v].size() - 1);
+    fl = std::max(fl, logs[v].back());
+  }
+  if (rep) {
+    rep->iterations = iters;
+    rep->final_log = fl;
+    rep->precond_applies = applies;
+    rep->converged = fl <= o->tol ? 1 : 0;
+    if (rep->log && rep->log_capacity > 0) {
+      rep->log_len = std::min<int>(rep->log_capacity, (int)logs[0].size());
+      for (int i = 0; i < rep->log_len; ++i) rep->log[i] = logs[0][i];
+    }
+  }
+  return LSW_OK;
+}
+
+static lsw_status gmres_flexible(lsw_ctx* ctx, const double2* b, double2* x, int nv, const lsw_gmres_opts* o,
+                                 lsw_gmres_report* rep, cudaStream_t st) {
+  const long long n2 = ctx->n2;
+  const size_t vb = (size_t)nv * n2 * sizeof(double2);
+  const int m = std::max(1, o->restart);
+  CK(ctx->k_basis.ensure(vb * (size_t)(m + 1)), "cudaMalloc(V)");
+  CK(ctx->k_zbasis.ensure(vb * (size_t)m), "cudaMalloc(Z)");
+  CK(ctx->k_tmp.ensure(vb), "cudaMalloc(tmp)");
+  CK(ctx->k_part.ensure((size_t)nv * 1216 * sizeof(double2)), "cudaMalloc(partials)");
+  CK(ctx->k_small.ensure((size_t)nv * (m + 2) * sizeof(double2) + 64), "cudaMalloc(h)");
+  CK(ctx->k_small2.ensure((size_t)nv * (m + 2) * sizeof(double2) + 64), "cudaMalloc(coef)");
+  CK(ctx->k_nrm.ensure((size_t)nv * 2 * sizeof(double2) + 64), "cudaMalloc(nrm)");
+  double2* V = ctx->k_basis.as<double2>();
+  double2* Z = ctx->k_zbasis.as<double2>();
+  double2* tmp = ctx->k_tmp.as<double2>();
+  double2* part = ctx->k_part.as<double2>();
+  double2* hdev = ctx->k_small.as<double2>();
+  double2* cdev = ctx->k_small2.as<double2>();
+  double* ndev = ctx->k_nrm.as<double>();
+  auto Vi = [&](int i) { return V + (size_t)i * nv * n2; };
+  auto Zi = [&](int i) { return Z + (size_t)i * nv * n2; };
+  lsw_status s;
+  int applies = 0, it = 0;
+  CK(cudaMemsetAsync(x, 0, vb, st), "x0 = 0");
+  CK(launch_norm2(b, n2, nv, n2, reinterpret_cast<double*>(part), ndev, st), "norm b");
+  std::vector<double> bn(nv);
+  CK(cudaMemcpyAsync(bn.data(), ndev, nv * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaStreamSynchronize(st), "sync");
+  for (auto& q : bn) q = std::sqrt(q);
+  std::vector<double> rel(nv, 1.0), log0;
+  std::vector<int> conv(nv, 0);
+  while (true) {
+    // r = b - A x
+    if ((s = apply_A_impl(ctx, x, tmp, nv, st)) != LSW_OK) return s;
+    for (int v = 0; v < nv; ++v) CK(launch_sub(Vi(0) + v * n2, b + v * n2, tmp + v * n2, n2, st), "sub");
+    CK(launch_norm2(Vi(0), n2, nv, n2, reinterpret_cast<double*>(part), ndev, st), "norm r");
+    std::vector<double> rn(nv);
+    CK(cudaMemcpyAsync(rn.data(), ndev, nv * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaStreamSynchronize(st), "sync");
+    std::vector<double2> sc(nv);
+    for (int v = 0; v < nv; ++v) {
+      rn[v] = std::sqrt(rn[v]);
+      rel[v] = bn[v] > 0 ? rn[v] / bn[v] : 0.0;
+      conv[v] = rel[v] <= o->tol ? 1 : 0;
+      sc[v] = make_double2(rn[v] > 0 ? rn[v] : 1.0, 0.0);
+    }
+    log0.push_back(rel[0]);
+    if (o->verbose) printf("fgmres it %d: true rel. residual %.6e\n", it, rel[0]);
+    if (std::all_of(conv.begin(), conv.end(), [](int c) { return c != 0; }) || it >= o->max_iter) break;
+    CK(cudaMemcpyAsync(cdev, sc.data(), nv * sizeof(double2), cudaMemcpyHostToDevice, st), "H2D");
+    CK(launch_scale(Vi(0), Vi(0), cdev, 1, n2, nv, n2, st), "scale");
+    std::vector<std::vector<cplx>> H(nv, std::vector<cplx>((size_t)(m + 1) * m)), g(nv, std::vector<cplx>(m + 1));
+    std::vector<std::vector<cplx>> cs(nv, std::vector<cplx>(m)), sn(nv, std::vector<cplx>(m));
+    std::vector<int> active(nv);
+    for (int v = 0; v < nv; ++v) { g[v][0] = rn[v]; active[v] = conv[v] ? 0 : 1; }
+    int ncol = 0;
+    for (int j = 0; j < m; ++j) {
+      if ((s = precond_impl(ctx, Vi(j), Zi(j), nv, st)) != LSW_OK) return s;
+      ++applies;
+      double2* w = Vi(j + 1);
+      if ((s = apply_A_impl(ctx, Zi(j), w, nv, st)) != LSW_OK) return s;
+      // MGS: h_i = V_i^H w ; w -= h_i V_i
+      CK(launch_dot(Vi(0), w, n2, nv, n2, part, hdev, st), "dot");
+      for (int i = 0; i <= j; ++i) {
+        if (i < j)
+          CK(launch_axpy_dot(w, Vi(i), hdev + (size_t)i * nv, Vi(i + 1), n2, nv, n2, part,
+                             hdev + (size_t)(i + 1) * nv, 0, st), "axpy_dot");
+        else
+          CK(launch_axpy_dot(w, Vi(i), hdev + (size_t)i * nv, nullptr, n2, nv, n2, part,
+                             hdev + (size_t)(j + 1) * nv, 0, st), "axpy_norm");
+      }
+      std::vector<double2> hh((size_t)(j + 2) * nv);
+      CK(cudaMemcpyAsync(hh.data(), hdev, hh.size() * sizeof(double2), cudaMemcpyDeviceToHost, st), "D2H h");
+      CK(cudaStreamSynchronize(st), "sync");
+      ++it;
+      ncol = j + 1;
+      bool all_small = true;
+      for (int v = 0; v < nv; ++v) {
+        std::vector<cplx> h(j + 2);
+        for (int i = 0; i <= j; ++i) h[i] = cplx(hh[(size_t)i * nv + v].x, hh[(size_t)i * nv + v].y);
+        const double hn_ = std::sqrt(hh[(size_t)(j + 1) * nv + v].x);
+        h[j + 1] = hn_;
+        sc[v] = make_double2(hn_ > 0 ? hn_ : 1.0, 0.0);
+        for (int i = 0; i < j; ++i) {
+          const cplx t = std::conj(cs[v][i]) * h[i] + std::conj(sn[v][i]) * h[i + 1];
+          h[i + 1] = -sn[v][i] * h[i] + cs[v][i] * h[i + 1];
+          h[i] = t;
+        }
+        const double den = std::sqrt(std::norm(h[j]) + std::norm(h[j + 1]));
+        cs[v][j] = den > 0 ? h[j] / den : cplx(1, 0);
+        sn[v][j] = den > 0 ? h[j + 1] / den : cplx(0, 0);
+        h[j] = den;
+        h[j + 1] = 0.0;
+        g[v][j + 1] = -sn[v][j] * g[v][j];
+        g[v][j] = std::conj(cs[v][j]) * g[v][j];
+        for (int i = 0; i <= j + 1; ++i) H[v][(size_t)i * m + j] = h[i];
+        const double est = bn[v] > 0 ? std::abs(g[v][j + 1]) / bn[v] : 0.0;
+        if (v == 0) log0.push_back(est);
+        if (active[v] && est > o->tol && hn_ > 0) all_small = false;
+      }
+      if (o->verbose) printf("fgmres it %d: estimate %.6e\n", it, log0.back());
+      CK(cudaMemcpyAsync(cdev, sc.data(), nv * sizeof(double2), cudaMemcpyHostToDevice, st), "H2D");
+      CK(launch_scale(w, w, cdev, 1, n2, nv, n2, st), "scale");
+      if (all_small || it >= o->max_iter) break;
+    }
+    // x += Z y  with y from the triangular system R y = g
+    std::vector<double2> coef((size_t)nv * ncol, make_double2(0, 0));
+    for (int v = 0; v < nv; ++v) {
+      if (!active[v]) continue;
+      std::vector<cplx> y(ncol);
+      for (int i = ncol - 1; i >= 0; --i) {
+        cplx sm = g[v][i];
+        for (int q = i + 1; q < ncol; ++q) sm -= H[v][(size_t)i * m + q] * y[q];
+        y[i] = H[v][(size_t)i * m + i] != cplx(0, 0) ? sm / H[v][(size_t)i * m + i] : cplx(0, 0);
+      }
+      for (int i = 0; i < ncol; ++i) coef[(size_t)v * ncol + i] = make_double2(y[i].real(), y[i].imag());
+    }
+    CK(ctx->k_small2.ensure(coef.size() * sizeof(double2) + 64), "cudaMalloc(coef)");
+    cdev = ctx->k_small2.as<double2>();
+    CK(cudaMemcpyAsync(cdev, coef.data(), coef.size() * sizeof(double2), cudaMemcpyHostToDevice, st), "H2D y");
+    CK(launch_lincomb(x, Z, (long long)nv * n2, n2, cdev, ncol, n2, nv, n2, st), "lincomb");
+  }
+  double worst = 0.0;
+  for (int v = 0; v < nv; ++v) worst = std::max(worst, rel[v]);
+  if (rep) {
+    rep->iterations = it;
+    rep->final_log = worst;
+    rep->precond_applies = applies;
+    rep->converged = worst <= o->tol ? 1 : 0;
+    if (rep->log && rep->log_capacity > 0) {
+      rep->log_len = std::min<int>(rep->log_capacity, (int)log0.size());
+      for (int i = 0; i < rep->log_len; ++i) rep->log[i] = log0[i];
+    }
+  }
+  return LSW_OK;
+}
+
+static lsw_status true_residual(lsw_ctx* ctx, const double2* b, const double2* x, int nv, double* worst,
+                                cudaStream_t st) {
+  const long long n2 = ctx->n2;
+  CK(ctx->k_tmp2.ensure((size_t)nv * n2 * sizeof(double2)), "cudaMalloc(res)");
+  CK(ctx->k_part.ensure((size_t)nv * 1216 * sizeof(double2)), "cudaMalloc(partials)");
+  CK(ctx->k_nrm.ensure((size_t)nv * 2 * sizeof(double2) + 64), "cudaMalloc(nrm)");
+  double2* r = ctx->k_tmp2.as<double2>();
+  lsw_status s = apply_A_impl(ctx, x, r, nv, st);
+  if (s != LSW_OK) return s;
+  for (int v = 0; v < nv; ++v) CK(launch_sub(r + v * n2, b + v * n2, r + v * n2, n2, st), "sub");
+  double* nd = ctx->k_nrm.as<double>();
+  CK(launch_norm2(r, n2, nv, n2, reinterpret_cast<double*>(ctx->k_part.p), nd, st), "norm");
+  CK(launch_norm2(b, n2, nv, n2, reinterpret_cast<double*>(ctx->k_part.p), nd + nv, st), "norm");
+  std::vector<double> h(2 * nv);
+  CK(cudaMemcpyAsync(h.data(), nd, 2 * nv * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaStreamSynchronize(st), "sync");
+  *worst = 0.0;
+  for (int v = 0; v < nv; ++v) *worst = std::max(*worst, h[nv + v] > 0 ? std::sqrt(h[v] / h[nv + v]) : 0.0);
+  return LSW_OK;
+}
+
+lsw_status lsw_gmres(lsw_ctx* ctx, const void* b, void* x, int nrhs, const lsw_gmres_opts* o, lsw_gmres_report* rep,
+                     void* stream) {
+  if (!ctx || !b || !x || !o || nrhs < 1) return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "bad arguments to lsw_gmres");
+  if (!ctx->is_setup) return fail(ctx, LSW_ERR_NOT_SET_UP, "lsw_problem_setup first");
+  if (!ctx->factorized) return fail(ctx, LSW_ERR_NOT_FACTORIZED, "lsw_factorize first");
+  if (o->max_iter < 0 || !(o->tol >= 0)) return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "bad GMRES options");
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  cudaStream_t st = S(stream);
+  const auto t0 = std::chrono::steady_clock::now();
+  const double2* bb = reinterpret_cast<const double2*>(b);
+  double2* xx = reinterpret_cast<double2*>(x);
+  lsw_status s;
+  if (o->mode == LSW_GMRES_REFERENCE) s = gmres_reference(ctx, bb, xx, nrhs, o, rep, st);
+  else if (o->mode == LSW_GMRES_FLEXIBLE) s = gmres_flexible(ctx, bb, xx, nrhs, o, rep, st);
+  else return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "unknown GMRES mode");
+  if (s != LSW_OK) return s;
+  double tr = 0.0;
+  if ((s = true_residual(ctx, bb, xx, nrhs, &tr, st)) != LSW_OK) return s;
+  CK(cudaStreamSynchronize(st), "sync");
+  const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (rep) { rep->true_rel_res = tr; rep->seconds = secs; }
+  return LSW_OK;
+}
+
+lsw_status lsw_solve_host(lsw_ctx* ctx, const double* b_host, double* x_host, int nrhs, const lsw_gmres_opts* o,
+                          lsw_gmres_report* rep, void* stream) {
+  if (!ctx || !b_host || !x_host || !o || nrhs < 1) return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "bad arguments to lsw_solve_host");
+  if (!ctx->is_setup) return fail(ctx, LSW_ERR_NOT_SET_UP, "lsw_problem_setup first");
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  cudaStream_t st = S(stream);
+  const size_t vb = (size_t)nrhs * ctx->n2 * sizeof(double2);
+  DevBuf db, dx;
+  CK(db.ensure(vb), "cudaMalloc(b)");
+  CK(dx.ensure(vb), "cudaMalloc(x)");
+  CK(cudaMemcpyAsync(db.p, b_host, vb, cudaMemcpyHostToDevice, st), "H2D b");
+  lsw_status s = lsw_gmres(ctx, db.p, dx.p, nrhs, o, rep, stream);
+  if (s != LSW_OK) return s;
+  CK(cudaMemcpyAsync(x_host, dx.p, vb, cudaMemcpyDeviceToHost, st), "D2H x");
+  CK(cudaStreamSynchronize(st), "sync");
+  return LSW_OK;
+}
+
+}  // extern "C"

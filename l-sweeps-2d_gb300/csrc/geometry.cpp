@@ -1,0 +1,315 @@
+// Host-side geometry of the checkerboard decomposition, PML coefficient
+// profiles and the sweep-front schedule.
+#include "internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <stdexcept>
+#include <tuple>
+
+namespace lsw {
+
+DirGeom dir_geom(int J, int N, int m, int p) {
+  // DDCheckerboard::setUp, DDCheckerboard.cpp:214-330: a = (m+1) J h, b = a + m h,
+  // left extension 2 tt h (J > 0), right extension 4 tt h (J < N-1), tt = 1.
+  DirGeom g{};
+  const int n_g = N * m + N - 1;
+  const int ka = (m + 1) * J, kb = ka + m;
+  const int lo = J > 0 ? ka - 2 : 0;
+  const int hi = J < N - 1 ? kb + 4 : n_g;
+  g.lo = lo;
+  g.nel = hi - lo;
+  g.nd = g.nel + 2 * p - 1;
+  auto loc = [&](int node) { return node - lo + p - 1; };
+  for (int s = 0; s < 2; ++s) {
+    const int off = 2 * s;  // shifted traces sit two rows further in (DDCheckerboard.cpp:227-230, 253-257)
+    g.lines[s][0] = J > 0 ? loc(ka - 1 + off) : -1;
+    g.lines[s][1] = J > 0 ? loc(ka + off) : -1;
+    g.lines[s][2] = J < N - 1 ? loc(kb + off) : -1;
+    g.lines[s][3] = J < N - 1 ? loc(kb + 1 + off) : -1;
+    // owned DOFs: trace1 .. traceN, open where the cell touches the domain boundary
+    // (mValsToKeep*, DDCheckerboard.cpp:446-634)
+    g.own[s][0] = J > 0 ? loc(ka + off) : 0;
+    g.own[s][1] = J < N - 1 ? loc(kb + off) : g.nd - 1;
+  }
+  return g;
+}
+
+bool geom_valid(const lsw_geom* g, std::string* why) {
+  if (!g) { *why = "geometry is NULL"; return false; }
+  if (g->order != 2) { *why = "only Order = 2 (5-point stencil) is supported"; return false; }
+  if (g->n_cells < 1) { *why = "n_cells must be >= 1"; return false; }
+  if (g->n_els_in_cell <= 4) { *why = "Not enough elements in cell (need > 4, DDCheckerboard.cpp:106-111)"; return false; }
+  if (g->pml < 1) { *why = "pml must be >= 1"; return false; }
+  if (!(g->h > 0.0) || !std::isfinite(g->h)) { *why = "h must be positive"; return false; }
+  int nd = 0;
+  for (int J = 0; J < g->n_cells; ++J) nd = std::max(nd, dir_geom(J, g->n_cells, g->n_els_in_cell, g->pml).nd);
+  if (nd > 256) { *why = "cell side exceeds 256 DOFs (m + 6 + 2p - 1 <= 256)"; return false; }
+  return true;
+}
+
+Profile1D make_profile(int nel, int p, double h, double C) {
+  // sigma = C ((dist into PML)/delta)^3, delta = p h; alpha = 1/(1 + i sigma),
+  // alpha' = -i sigma' / (1 + i sigma)^2 (PMLCubic2D.cpp:67-236); Lambda = alpha^2
+  // (diffusion), beta = alpha' alpha (convection); second/first derivative
+  // stencils [1 -2 1]/h^2 and [-1 0 1]/(2h) (FiniteDifferences.cpp:57-122).
+  const int nd = nel + 2 * p - 1;
+  Profile1D pr;
+  pr.lo_re.resize(nd); pr.lo_im.resize(nd); pr.hi_re.resize(nd); pr.hi_im.resize(nd);
+  pr.dg_re.resize(nd); pr.dg_im.resize(nd);
+  const std::complex<double> I(0.0, 1.0);
+  const double p3 = double(p) * p * p;
+  for (int i = 0; i < nd; ++i) {
+    const int q = i + 1;  // nodes from the start of the computational domain
+    double sg = 0.0, dsg = 0.0;
+    if (q < p) {
+      const double d = double(p - q);
+      sg = C * std::pow(d / p, 3.0);
+      dsg = -3.0 * C * d * d / (p3 * h);
+    } else if (q > p + nel) {
+      const double d = double(q - p - nel);
+      sg = C * std::pow(d / p, 3.0);
+      dsg = 3.0 * C * d * d / (p3 * h);
+    }
+    const std::complex<double> a = 1.0 / (1.0 + I * sg);
+    const std::complex<double> ad = -I * dsg / std::pow(1.0 + I * sg, 2.0);
+    const std::complex<double> lam = std::pow(a, 2.0);
+    const std::complex<double> beta = ad * a;
+    const double h2 = h * h;
+    const std::complex<double> lo = -lam / h2 + beta / (2.0 * h);
+    const std::complex<double> hi = -lam / h2 - beta / (2.0 * h);
+    const std::complex<double> dg = 2.0 * lam / h2;
+    pr.lo_re[i] = lo.real(); pr.lo_im[i] = lo.imag();
+    pr.hi_re[i] = hi.real(); pr.hi_im[i] = hi.imag();
+    pr.dg_re[i] = dg.real(); pr.dg_im[i] = dg.imag();
+  }
+  return pr;
+}
+
+// ---------------------------------------------------------------------------
+// Schedule.  Restates the cell visiting order of DDCheckerboard::applySweep
+// (DDCheckerboard.cpp:812-880): stage 1 (addLocSol) is one front; the four
+// stage-2 sweeps (addRight/Left/Up/DownSweep) advance one column/row per
+// front; the four stage-3 L-sweeps (addBL2TR/TR2BL/BR2TL/TL2BRSweep) advance
+// one anti-diagonal per front.  The four shifted decompositions of
+// applyPrecond (687-739) and every right-hand side share each front.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct SlotSpec {
+  DevSlot s;
+  int rhs, shift, order;
+};
+
+DevSlot blank_slot() {
+  DevSlot s{};
+  s.in_lr0 = s.in_lr1 = s.in_ud0 = s.in_ud1 = -1;
+  for (int i = 0; i < 4; ++i) { s.lr_out[i] = -1; s.ud_out[i] = -1; s.lr_line[i] = -1; s.ud_line[i] = -1; }
+  return s;
+}
+
+}  // namespace
+
+void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, int rmax, long long LP,
+                    std::vector<Front>& fronts, std::vector<DevItem>& items, std::vector<DevSlot>& slots,
+                    std::vector<DevGroup>& groups, long long n_dof2) {
+  const int nc = (int)cells.size();
+  auto cid = [&](int I, int J) { return I * N + J; };
+  auto toff = [&](int rhs, int s, int c, int set, int line) { return trace_off(rhs, s, c, set, line, nc, LP); };
+
+  // per front: map cell -> list of slot specs
+  std::vector<std::map<int, std::vector<SlotSpec>>> fr;
+
+  // ---- stage 1 ----
+  {
+    std::map<int, std::vector<SlotSpec>> f;
+    for (int c = 0; c < nc; ++c) {
+      const DevCell& cl = cells[c];
+      for (int r = 0; r < nrhs; ++r)
+        for (int s = 0; s < 4; ++s) {
+          DevSlot d = blank_slot();
+          d.kind = SK_VOLUME; d.shift = s; d.rhs = r;
+          const int sx = s & 1, sy = (s >> 1) & 1;
+          for (int l = 0; l < 4; ++l) {
+            if (cl.lx[sx][l] >= 0) { d.lr_line[d.n_lr] = cl.lx[sx][l]; d.lr_out[d.n_lr] = toff(r, s, c, TS_LR, l); d.n_lr++; }
+            if (cl.ly[sy][l] >= 0) { d.ud_line[d.n_ud] = cl.ly[sy][l]; d.ud_out[d.n_ud] = toff(r, s, c, TS_UD, l); d.n_ud++; }
+          }
+          f[c].push_back({d, r, s, 0});
+        }
+    }
+    fr.push_back(std::move(f));
+  }
+
+  // ---- stage 2 ----
+  for (int t = 1; t < N; ++t) {
+    std::map<int, std::vector<SlotSpec>> f;
+    for (int r = 0; r < nrhs; ++r)
+      for (int s = 0; s < 4; ++s) {
+        const int sx = s & 1, sy = (s >> 1) & 1;
+        for (int k = 0; k < N; ++k) {
+          // right sweep (addRightSweep 1168-1350): cell (k, t), source on trace0/trace1
+          {
+            const int c = cid(k, t), nb = cid(k, t - 1);
+            const DevCell& cl = cells[c];
+            DevSlot d = blank_slot();
+            d.kind = SK_DIR_X; d.shift = s; d.rhs = r;
+            d.xo = cl.lx[sx][0]; d.xi = cl.lx[sx][1]; d.dx = 1;
+            d.in_lr0 = toff(r, s, nb, TS_LR, 2); d.in_lr1 = toff(r, s, nb, TS_LR, 3);
+            for (int l = 0; l < 4; ++l)
+              if (cl.ly[sy][l] >= 0) { d.ud_line[d.n_ud] = cl.ly[sy][l]; d.ud_out[d.n_ud] = toff(r, s, c, TS_UDRIGHT, l); d.n_ud++; }
+            for (int l = 2; l < 4; ++l)
+              if (cl.lx[sx][l] >= 0) { d.lr_line[d.n_lr] = cl.lx[sx][l]; d.lr_out[d.n_lr] = toff(r, s, c, TS_LR, l); d.n_lr++; }
+            f[c].push_back({d, r, s, 0});
+          }
+          // left sweep (addLeftSweep 976-1164): cell (k, N-1-t), source on traceN/traceNP
+          {
+            const int J = N - 1 - t;
+            const int c = cid(k, J), nb = cid(k, J + 1);
+            const DevCell& cl = cells[c];
+            DevSlot d = blank_slot();
+            d.kind = SK_DIR_X; d.shift = s; d.rhs = r;
+            d.xo = cl.lx[sx][3]; d.xi = cl.lx[sx][2]; d.dx = -1;
+            d.in_lr0 = toff(r, s, nb, TS_LR, 1); d.in_lr1 = toff(r, s, nb, TS_LR, 0);
+            for (int l = 0; l < 4; ++l)
+              if (cl.ly[sy][l] >= 0) { d.ud_line[d.n_ud] = cl.ly[sy][l]; d.ud_out[d.n_ud] = toff(r, s, c, TS_UDLEFT, l); d.n_ud++; }
+            for (int l = 0; l < 2; ++l)
+              if (cl.lx[sx][l] >= 0) { d.lr_line[d.n_lr] = cl.lx[sx][l]; d.lr_out[d.n_lr] = toff(r, s, c, TS_LR, l); d.n_lr++; }
+            f[c].push_back({d, r, s, 1});
+          }
+          // up sweep (addUpSweep 1544-1724): cell (t, k), source on trace0/trace1 rows
+          {
+            const int c = cid(t, k), nb = cid(t - 1, k);
+            const DevCell& cl = cells[c];
+            DevSlot d = blank_slot();
+            d.kind = SK_DIR_Y; d.shift = s; d.rhs = r;
+            d.yo = cl.ly[sy][0]; d.yi = cl.ly[sy][1]; d.dy = 1;
+            d.in_ud0 = toff(r, s, nb, TS_UD, 2); d.in_ud1 = toff(r, s, nb, TS_UD, 3);
+            for (int l = 0; l < 4; ++l)
+              if (cl.lx[sx][l] >= 0) { d.lr_line[d.n_lr] = cl.lx[sx][l]; d.lr_out[d.n_lr] = toff(r, s, c, TS_LRUP, l); d.n_lr++; }
+            for (int l = 2; l < 4; ++l)
+              if (cl.ly[sy][l] >= 0) { d.ud_line[d.n_ud] = cl.ly[sy][l]; d.ud_out[d.n_ud] = toff(r, s, c, TS_UD, l); d.n_ud++; }
+            f[c].push_back({d, r, s, 2});
+          }
+          // down sweep (addDownSweep 1353-1540): cell (N-1-t, k), source on traceN/traceNP rows
+          {
+            const int I = N - 1 - t;
+            const int c = cid(I, k), nb = cid(I + 1, k);
+            const DevCell& cl = cells[c];
+            DevSlot d = blank_slot();
+            d.kind = SK_DIR_Y; d.shift = s; d.rhs = r;
+            d.yo = cl.ly[sy][3]; d.yi = cl.ly[sy][2]; d.dy = -1;
+            d.in_ud0 = toff(r, s, nb, TS_UD, 1); d.in_ud1 = toff(r, s, nb, TS_UD, 0);
+            for (int l = 0; l < 4; ++l)
+              if (cl.lx[sx][l] >= 0) { d.lr_line[d.n_lr] = cl.lx[sx][l]; d.lr_out[d.n_lr] = toff(r, s, c, TS_LRDOWN, l); d.n_lr++; }
+            for (int l = 0; l < 2; ++l)
+              if (cl.ly[sy][l] >= 0) { d.ud_line[d.n_ud] = cl.ly[sy][l]; d.ud_out[d.n_ud] = toff(r, s, c, TS_UD, l); d.n_ud++; }
+            f[c].push_back({d, r, s, 3});
+          }
+        }
+      }
+    fr.push_back(std::move(f));
+  }
+
+  // ---- stage 3 ----
+  struct LS { int lrbuf, udbuf, xr, yt; };  // xr: incoming from the right, yt: from the top
+  const LS lsw_[4] = {
+      {TS_LRUP, TS_UDRIGHT, 0, 0},    // BL2TR (2393-2608)
+      {TS_LRDOWN, TS_UDLEFT, 1, 1},   // TR2BL (1949-2170)
+      {TS_LRUP, TS_UDLEFT, 1, 0},     // BR2TL (2173-2390)
+      {TS_LRDOWN, TS_UDRIGHT, 0, 1},  // TL2BR (1727-1946)
+  };
+  for (int dd = 0; dd <= 2 * N - 4; ++dd) {
+    std::map<int, std::vector<SlotSpec>> f;
+    for (int r = 0; r < nrhs; ++r)
+      for (int s = 0; s < 4; ++s) {
+        const int sx = s & 1, sy = (s >> 1) & 1;
+        for (int w = 0; w < 4; ++w) {
+          const LS& L = lsw_[w];
+          for (int I = 0; I < N; ++I)
+            for (int J = 0; J < N; ++J) {
+              const int ii = L.yt ? N - 1 - I : I;
+              const int jj = L.xr ? N - 1 - J : J;
+              if (ii < 1 || jj < 1 || ii + jj - 2 != dd) continue;
+              const int c = cid(I, J);
+              const DevCell& cl = cells[c];
+              DevSlot d = blank_slot();
+              d.kind = SK_CORNER; d.shift = s; d.rhs = r; d.overwrite = 1;
+              if (!L.xr) {
+                const int nb = cid(I, J - 1);
+                d.xo = cl.lx[sx][0]; d.xi = cl.lx[sx][1]; d.dx = 1;
+                d.in_lr0 = toff(r, s, nb, L.lrbuf, 2); d.in_lr1 = toff(r, s, nb, L.lrbuf, 3);
+                for (int l = 2; l < 4; ++l)
+                  if (cl.lx[sx][l] >= 0) { d.lr_line[d.n_lr] = cl.lx[sx][l]; d.lr_out[d.n_lr] = toff(r, s, c, L.lrbuf, l); d.n_lr++; }
+              } else {
+                const int nb = cid(I, J + 1);
+                d.xo = cl.lx[sx][3]; d.xi = cl.lx[sx][2]; d.dx = -1;
+                d.in_lr0 = toff(r, s, nb, L.lrbuf, 1); d.in_lr1 = toff(r, s, nb, L.lrbuf, 0);
+                for (int l = 0; l < 2; ++l)
+                  if (cl.lx[sx][l] >= 0) { d.lr_line[d.n_lr] = cl.lx[sx][l]; d.lr_out[d.n_lr] = toff(r, s, c, L.lrbuf, l); d.n_lr++; }
+              }
+              if (!L.yt) {
+                const int nb = cid(I - 1, J);
+                d.yo = cl.ly[sy][0]; d.yi = cl.ly[sy][1]; d.dy = 1;
+                d.in_ud0 = toff(r, s, nb, L.udbuf, 2); d.in_ud1 = toff(r, s, nb, L.udbuf, 3);
+                for (int l = 2; l < 4; ++l)
+                  if (cl.ly[sy][l] >= 0) { d.ud_line[d.n_ud] = cl.ly[sy][l]; d.ud_out[d.n_ud] = toff(r, s, c, L.udbuf, l); d.n_ud++; }
+              } else {
+                const int nb = cid(I + 1, J);
+                d.yo = cl.ly[sy][3]; d.yi = cl.ly[sy][2]; d.dy = -1;
+                d.in_ud0 = toff(r, s, nb, L.udbuf, 1); d.in_ud1 = toff(r, s, nb, L.udbuf, 0);
+                for (int l = 0; l < 2; ++l)
+                  if (cl.ly[sy][l] >= 0) { d.ud_line[d.n_ud] = cl.ly[sy][l]; d.ud_out[d.n_ud] = toff(r, s, c, L.udbuf, l); d.n_ud++; }
+              }
+              f[c].push_back({d, r, s, w});
+            }
+        }
+      }
+    fr.push_back(std::move(f));
+  }
+
+  // ---- flatten into items (whole (shift, rhs) groups, at most rmax slots) ----
+  fronts.clear(); items.clear(); slots.clear(); groups.clear();
+  for (auto& f : fr) {
+    Front F{(int)items.size(), 0, 0};
+    for (auto& kv : f) {
+      const int c = kv.first;
+      auto& v = kv.second;
+      std::stable_sort(v.begin(), v.end(), [](const SlotSpec& a, const SlotSpec& b) {
+        return std::make_tuple(a.rhs, a.shift, a.order) < std::make_tuple(b.rhs, b.shift, b.order);
+      });
+      size_t i = 0;
+      while (i < v.size()) {
+        DevItem it{};
+        it.cell = c;
+        it.slot_begin = (int)slots.size();
+        it.group_begin = (int)groups.size();
+        while (i < v.size()) {
+          size_t j = i;
+          while (j < v.size() && v[j].rhs == v[i].rhs && v[j].shift == v[i].shift) ++j;
+          const int gsz = int(j - i);
+          if (gsz > rmax) throw std::runtime_error("sweep group larger than the slot capacity of a front item");
+          if (it.slot_count > 0 && it.slot_count + gsz > rmax) break;
+          DevGroup g{};
+          g.slot_begin = (int)slots.size() - it.slot_begin;
+          g.slot_count = gsz;
+          g.shift = v[i].shift;
+          g.out_off = ((long long)v[i].rhs * 4 + v[i].shift) * n_dof2;
+          groups.push_back(g);
+          for (size_t q = i; q < j; ++q) slots.push_back(v[q].s);
+          it.slot_count += gsz;
+          it.group_count++;
+          i = j;
+        }
+        const DevCell& cl = cells[c];
+        it.scratch_off = F.scratch_elems;
+        F.scratch_elems += (long long)cl.nx * it.slot_count * cl.ldn;
+        items.push_back(it);
+        F.item_count++;
+      }
+    }
+    fronts.push_back(F);
+  }
+}
+
+}  // namespace lsw

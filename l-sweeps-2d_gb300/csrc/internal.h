@@ -1,0 +1,170 @@
+// Internal types of the GB300 L-sweeps library: cell geometry on the integer
+// grid, device cell table, sweep-front descriptors, and the kernel launchers.
+#pragma once
+#include "lsweeps.h"
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+#include <map>
+
+namespace lsw {
+
+// ---------------------------------------------------------------------------
+// Geometry along one direction for cell index J (column J along x, row I along
+// y).  Integer-grid restatement of DDCheckerboard::setUp (DDCheckerboard.cpp:
+// 214-330, 388-419) and SubdomainStructured::assignIndexSets (1019-1116) for
+// Order = 2 (trace thickness 1, DDCheckerboard.cpp:104):
+//   global nodes k = 0..n_g, k_a = (m+1) J, k_b = k_a + m;
+//   interior domain [k_a - 2, k_b + 4], clipped to [0, n_g] at the boundary;
+//   local DOF i <-> global DOF lo + i; nd = (hi - lo) + 2p - 1 DOFs;
+//   traces (non-shifted) t0 = k_a-1, t1 = k_a, tN = k_b, tNP = k_b+1,
+//   (shifted) the same + 2; owned [k_a, k_b] (+2 shifted), open at the
+//   domain boundary.
+// ---------------------------------------------------------------------------
+struct DirGeom {
+  int lo;            // global node index of the interior-domain start == global DOF of local 0
+  int nel;           // interior elements of the cell
+  int nd;            // DOFs per side: nel + 2p - 1
+  int lines[2][4];   // local index of t0, t1, tN, tNP ([shift]); -1 if absent
+  int own[2][2];     // owned local range [lo, hi] ([shift])
+};
+DirGeom dir_geom(int J, int N, int m, int p);
+bool geom_valid(const lsw_geom* g, std::string* why);
+
+// Separable coefficient profiles of the 5-point PML operator along one
+// direction of a box with `nel` interior elements and p PML cells
+// (PMLCubic2D.cpp:35-236; AssemblerHelmholtz2DFD.cpp:371-457):
+//   lo[k]  coupling to k-1  (-Lambda/h^2 + beta/(2h))
+//   hi[k]  coupling to k+1  (-Lambda/h^2 - beta/(2h))
+//   dg[k]  diagonal share    2 Lambda / h^2
+struct Profile1D {
+  std::vector<double> lo_re, lo_im, hi_re, hi_im, dg_re, dg_im;
+};
+Profile1D make_profile(int nel, int p, double h, double C);
+
+// ---------------------------------------------------------------------------
+// Device cell table.
+// ---------------------------------------------------------------------------
+struct DevCell {
+  int I, J;
+  int nx, ny;          // x-lines (block count) and points per line (block size)
+  int lox, loy;        // global DOF of local (0, 0)
+  int ldn;             // leading dimension of a factor block (column-major)
+  int pad0;
+  int lx[2][4], ly[2][4];
+  int ownx[2][2], owny[2][2];
+  long long fac_off;   // element offset of block 0 in the factor pool
+  long long prof_off;  // offset into the profile array: x-profiles (3*nx), then y (3*ny)
+};
+
+enum SlotKind : int {
+  SK_VOLUME = 0,   // stage 1: window of the global input restricted to the owned set
+  SK_DIR_X = 1,    // two-line equivalent source on x-lines (left/right sweeps)
+  SK_DIR_Y = 2,    // two-line equivalent source on y-rows (up/down sweeps)
+  SK_CORNER = 3,   // L-shaped equivalent source (stage 3)
+  SK_CELLVEC = 4   // full cell vector (LocalLinearSolver::solve)
+};
+
+// One right-hand side of a cell solve inside a sweep front.
+struct DevSlot {
+  int kind, shift, rhs, pad0;
+  int xo, xi, dx, yo, yi, dy;   // outer/inner source lines and their inward direction
+  int overwrite;                // L-sweep: trace0 lines take the incoming values (see DDCheckerboard.cpp:2520-2526)
+  int n_lr, n_ud;
+  int lr_line[4], ud_line[4];   // outgoing trace lines (local index)
+  long long in_lr0, in_lr1, in_ud0, in_ud1;   // trace-pool offsets of incoming lines, -1 if none
+  long long lr_out[4], ud_out[4];             // trace-pool offsets of outgoing lines
+};
+
+// A set of slots of one item that accumulate into the same output vector.
+struct DevGroup {
+  int slot_begin, slot_count, shift, pad0;
+  long long out_off;   // element offset of the output vector in the out pool; -1: none
+};
+
+struct DevItem {
+  int cell, slot_begin, slot_count, group_begin, group_count, pad0;
+  long long scratch_off;   // element offset of the item's forward-sweep storage
+};
+
+// A launch = one sweep front.
+struct Front {
+  int item_begin, item_count;
+  long long scratch_elems;
+};
+
+struct Schedule {
+  int nrhs = 0;
+  std::vector<Front> fronts;
+  DevItem* d_items = nullptr;
+  DevSlot* d_slots = nullptr;
+  DevGroup* d_groups = nullptr;
+  long long scratch_elems = 0;   // max over fronts
+  int max_slots = 0;
+};
+
+// Build the sweep schedule (stage 1, N-1 stage-2 fronts, 2N-3 stage-3 fronts,
+// all four shifted decompositions and nrhs right-hand sides in every front).
+void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, int rmax, long long LP,
+                    std::vector<Front>& fronts, std::vector<DevItem>& items, std::vector<DevSlot>& slots,
+                    std::vector<DevGroup>& groups, long long n_dof2);
+
+// Trace pool index of (rhs, shift, cell, set, line), in elements of stride LP.
+enum TraceSet : int { TS_LR = 0, TS_UD = 1, TS_LRUP = 2, TS_LRDOWN = 3, TS_UDRIGHT = 4, TS_UDLEFT = 5 };
+inline long long trace_off(int rhs, int s, int c, int set, int line, int ncell, long long LP) {
+  return ((((long long)rhs * 4 + s) * ncell + c) * 6 + set) * 4 * LP + (long long)line * LP;
+}
+
+// ---------------------------------------------------------------------------
+// Kernel launchers (defined in the .cu files).
+// ---------------------------------------------------------------------------
+struct FrontArgs {
+  const DevCell* cells;
+  const DevItem* items;
+  const DevSlot* slots;
+  const DevGroup* groups;
+  const void* fac;        // factor pool (cx_t<T>)
+  const double2* prof;    // profiles
+  void* traces;           // trace pool (cx_t<T>)
+  void* outs;             // out pool (cx_t<T>)
+  void* scratch;          // forward storage (cx_t<T>)
+  const double2* x_in;    // global input vectors (VOLUME) or cell vectors (CELLVEC)
+  long long x_stride;
+  double2* x_out;         // CELLVEC output
+  long long out_stride;
+  int n_dof, N, m, p;
+  int item_count;
+};
+
+template <typename T> cudaError_t launch_front(const FrontArgs& a, int max_ny, cudaStream_t st);
+template <typename T> cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* prof,
+                                                   const double* mgrid, int n_dof, double omega2,
+                                                   void* fac, void* work, int max_ny, int* status,
+                                                   cudaStream_t st);
+size_t factor_smem_bytes(int ny, bool dbl);
+
+cudaError_t launch_apply_A(const double2* x, double2* y, int nrhs, int n_dof, const double2* gprof,
+                           const double* mgrid, double omega2, cudaStream_t st);
+template <typename T> cudaError_t launch_combine(const void* outs, double2* y, int nrhs, long long n2,
+                                                 cudaStream_t st);
+cudaError_t launch_rhs(double2* b, int n_dof, int p, double h, const double* src, const double* amp,
+                       int nsrc, double eps, cudaStream_t st);
+
+// FP64 Krylov helpers; results of reductions land in device memory.
+cudaError_t launch_dot(const double2* a, const double2* b, long long n, int nvec, long long stride,
+                       double2* partial, double2* out, cudaStream_t st);   // out[v] = sum conj(a) b
+cudaError_t launch_norm2(const double2* a, long long n, int nvec, long long stride, double* partial,
+                         double* out, cudaStream_t st);                   // out[v] = sum |a|^2
+// y[v] = y[v] - coef[v] * x[v]; and (optionally) partial dot of conj(y_new) . z (dotout)
+cudaError_t launch_axpy_dot(double2* y, const double2* x, const double2* coef, const double2* z,
+                            long long n, int nvec, long long stride, double2* partial, double2* dotout,
+                            int conj_first_y, cudaStream_t st);
+cudaError_t launch_scale(double2* y, const double2* x, const double2* coef, int invert, long long n,
+                         int nvec, long long stride, cudaStream_t st);    // y = x*coef or x/coef
+cudaError_t launch_lincomb(double2* y, const double2* basis, long long basis_stride_vec,
+                           long long basis_stride_rhs, const double2* coef, int ncoef, long long n,
+                           int nvec, long long y_stride, cudaStream_t st); // y[v] += sum_i coef[v][i] basis[i][v]
+cudaError_t launch_sub(double2* y, const double2* a, const double2* b, long long n, cudaStream_t st);
+
+}  // namespace lsw

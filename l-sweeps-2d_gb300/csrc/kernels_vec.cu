@@ -1,0 +1,273 @@
+// Global-grid kernels: the FP64 5-point operator, the source assembly, the
+// sum of the four shifted sweeps, and the FP64 Krylov reductions.
+#include "common.cuh"
+#include "internal.h"
+
+namespace lsw {
+
+namespace {
+
+constexpr int kVT = 256;
+constexpr int kRedBlocks = 1216;   // 8 x 152 SMs
+
+// y = A x on the global grid (DDCheckerboard::applySystemMatrix equals the
+// globally assembled operator, DDCheckerboard.cpp:2611-2635).  Coefficients are
+// rebuilt from the separable PML profile (one profile serves x and y on the
+// square grid) and the squared slowness: 40 algorithmic bytes per DOF.
+__global__ void k_apply_A(const double2* __restrict__ x, double2* __restrict__ y, int n,
+                          const double2* __restrict__ gp, const double* __restrict__ m, double omega2,
+                          long long n2) {
+  const long long G = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int v = blockIdx.y;
+  if (G >= n2) return;
+  const int gx = (int)(G / n), gy = (int)(G - (long long)gx * n);
+  const double2* xv = x + (long long)v * n2;
+  const double2 lox = gp[gx], hix = gp[n + gx], dgx = gp[2 * n + gx];
+  const double2 loy = gp[gy], hiy = gp[n + gy], dgy = gp[2 * n + gy];
+  double2 c = cadd(dgx, dgy);
+  c.x -= omega2 * m[G];
+  double2 acc = cmul(c, xv[G]);
+  if (gx > 0) cfma(acc, lox, xv[G - n]);
+  if (gx < n - 1) cfma(acc, hix, xv[G + n]);
+  if (gy > 0) cfma(acc, loy, xv[G - 1]);
+  if (gy < n - 1) cfma(acc, hiy, xv[G + 1]);
+  y[(long long)v * n2 + G] = acc;
+}
+
+// M^-1 x = res1 + (res2 + res3 + res4)  (DDCheckerboard.cpp:733-735)
+template <typename T>
+__global__ void k_combine(const cx_t<T>* __restrict__ o, double2* __restrict__ y, long long n2) {
+  const long long G = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int v = blockIdx.y;
+  if (G >= n2) return;
+  const cx_t<T>* b = o + (long long)v * 4 * n2;
+  const double2 z = make_double2(0, 0);
+  const double2 a0 = to_c(b[G], z), a1 = to_c(b[n2 + G], z), a2 = to_c(b[2 * n2 + G], z),
+                a3 = to_c(b[3 * n2 + G], z);
+  y[(long long)v * n2 + G] = cadd(a0, cadd(cadd(a1, a2), a3));
+}
+
+// RHSSrcPts::eval (RHSSrcPts.cpp:87-112): sum of 1/(pi eps^2) exp(-|x-x0|^2/eps^2).
+__global__ void k_rhs(double2* __restrict__ b, int n, int p, double h, const double* __restrict__ src,
+                      const double* __restrict__ amp, int nsrc, double eps) {
+  const long long G = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (G >= (long long)n * n) return;
+  const int gx = (int)(G / n), gy = (int)(G - (long long)gx * n);
+  const double X = (gx + 1 - p) * h, Y = (gy + 1 - p) * h;
+  const double pi = 3.14159265358979323846;
+  double acc = 0.0;
+  for (int s = 0; s < nsrc; ++s) {
+    const double dx = src[2 * s] - X, dy = src[2 * s + 1] - Y;
+    acc += (amp ? amp[s] : 1.0) * (1.0 / (pi * eps * eps) * exp(-(dx * dx + dy * dy) / (eps * eps)));
+  }
+  b[G] = make_double2(acc, 0.0);
+}
+
+template <typename V>
+__device__ __forceinline__ V block_sum(V v, V* sh) {
+  // sum over the block (kVT threads), result valid in thread 0
+  for (int off = 16; off > 0; off >>= 1) {
+    if constexpr (sizeof(V) == 16) {
+      v.x += __shfl_down_sync(0xffffffffu, v.x, off);
+      v.y += __shfl_down_sync(0xffffffffu, v.y, off);
+    } else {
+      v += __shfl_down_sync(0xffffffffu, v, off);
+    }
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    V z{};
+    v = (l < (int)(blockDim.x >> 5)) ? sh[l] : z;
+    for (int off = 16; off > 0; off >>= 1) {
+      if constexpr (sizeof(V) == 16) {
+        v.x += __shfl_down_sync(0xffffffffu, v.x, off);
+        v.y += __shfl_down_sync(0xffffffffu, v.y, off);
+      } else {
+        v += __shfl_down_sync(0xffffffffu, v, off);
+      }
+    }
+  }
+  return v;
+}
+
+// partial[v][blk] = sum conj(a) b over the block's share
+__global__ void k_dot_partial(const double2* __restrict__ a, const double2* __restrict__ b, long long n,
+                              long long stride, double2* __restrict__ partial) {
+  __shared__ double2 sh[32];
+  const int v = blockIdx.y;
+  const double2* av = a + (long long)v * stride;
+  const double2* bv = b + (long long)v * stride;
+  double2 s = make_double2(0, 0);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double2 x = av[i], y = bv[i];
+    s.x += x.x * y.x + x.y * y.y;
+    s.y += x.x * y.y - x.y * y.x;
+  }
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) partial[(long long)v * gridDim.x + blockIdx.x] = s;
+}
+
+__global__ void k_finish2(const double2* __restrict__ partial, int nb, double2* __restrict__ out) {
+  __shared__ double2 sh[32];
+  const int v = blockIdx.x;
+  double2 s = make_double2(0, 0);
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) s = cadd(s, partial[(long long)v * nb + i]);
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) out[v] = s;
+}
+
+__global__ void k_norm2_partial(const double2* __restrict__ a, long long n, long long stride,
+                                double* __restrict__ partial) {
+  __shared__ double sh[32];
+  const int v = blockIdx.y;
+  const double2* av = a + (long long)v * stride;
+  double s = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    s += abs2(av[i]);
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) partial[(long long)v * gridDim.x + blockIdx.x] = s;
+}
+
+__global__ void k_finish1(const double* __restrict__ partial, int nb, double* __restrict__ out) {
+  __shared__ double sh[32];
+  const int v = blockIdx.x;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) s += partial[(long long)v * nb + i];
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) out[v] = s;
+}
+
+// y -= coef[v] x ; optional partial dot with z of the updated y:
+//   conj_first_y: sum conj(y) z   else: sum conj(z) y
+__global__ void k_axpy_dot(double2* __restrict__ y, const double2* __restrict__ x,
+                           const double2* __restrict__ coef, const double2* __restrict__ z, long long n,
+                           long long stride, double2* __restrict__ partial, int conj_first_y) {
+  __shared__ double2 sh[32];
+  const int v = blockIdx.y;
+  double2* yv = y + (long long)v * stride;
+  const double2* xv = x + (long long)v * stride;
+  const double2* zv = z ? z + (long long)v * stride : nullptr;
+  const double2 c = coef[v];
+  double2 s = make_double2(0, 0);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double2 t = yv[i];
+    cfms(t, c, xv[i]);
+    yv[i] = t;
+    if (zv) {
+      const double2 q = zv[i];
+      if (conj_first_y) { s.x += t.x * q.x + t.y * q.y; s.y += t.x * q.y - t.y * q.x; }
+      else { s.x += q.x * t.x + q.y * t.y; s.y += q.x * t.y - q.y * t.x; }
+    } else {
+      s.x += abs2(t);
+    }
+  }
+  if (partial) {
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) partial[(long long)v * gridDim.x + blockIdx.x] = s;
+  }
+}
+
+__global__ void k_scale(double2* __restrict__ y, const double2* __restrict__ x, const double2* __restrict__ coef,
+                        int invert, long long n, long long stride) {
+  const int v = blockIdx.y;
+  double2 c = coef[v];
+  if (invert) c = crcp(c);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[(long long)v * stride + i] = cmul(c, x[(long long)v * stride + i]);
+}
+
+__global__ void k_lincomb(double2* __restrict__ y, const double2* __restrict__ basis, long long bsv,
+                          long long bsr, const double2* __restrict__ coef, int ncoef, long long n,
+                          long long ys) {
+  const int v = blockIdx.y;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double2 acc = y[(long long)v * ys + i];
+    for (int q = 0; q < ncoef; ++q) cfma(acc, coef[(long long)v * ncoef + q], basis[q * bsv + v * bsr + i]);
+    y[(long long)v * ys + i] = acc;
+  }
+}
+
+__global__ void k_sub(double2* __restrict__ y, const double2* __restrict__ a, const double2* __restrict__ b,
+                      long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = csub(a[i], b[i]);
+}
+
+inline unsigned nblk(long long n) {
+  long long b = (n + kVT - 1) / kVT;
+  if (b > kRedBlocks) b = kRedBlocks;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+}  // namespace
+
+cudaError_t launch_apply_A(const double2* x, double2* y, int nrhs, int n_dof, const double2* gprof,
+                           const double* mgrid, double omega2, cudaStream_t st) {
+  const long long n2 = (long long)n_dof * n_dof;
+  dim3 g((unsigned)((n2 + kVT - 1) / kVT), nrhs);
+  k_apply_A<<<g, kVT, 0, st>>>(x, y, n_dof, gprof, mgrid, omega2, n2);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_combine(const void* outs, double2* y, int nrhs, long long n2, cudaStream_t st) {
+  dim3 g((unsigned)((n2 + kVT - 1) / kVT), nrhs);
+  k_combine<T><<<g, kVT, 0, st>>>(reinterpret_cast<const cx_t<T>*>(outs), y, n2);
+  return cudaGetLastError();
+}
+template cudaError_t launch_combine<float>(const void*, double2*, int, long long, cudaStream_t);
+template cudaError_t launch_combine<double>(const void*, double2*, int, long long, cudaStream_t);
+
+cudaError_t launch_rhs(double2* b, int n_dof, int p, double h, const double* src, const double* amp, int nsrc,
+                       double eps, cudaStream_t st) {
+  const long long n2 = (long long)n_dof * n_dof;
+  k_rhs<<<(unsigned)((n2 + kVT - 1) / kVT), kVT, 0, st>>>(b, n_dof, p, h, src, amp, nsrc, eps);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dot(const double2* a, const double2* b, long long n, int nvec, long long stride,
+                       double2* partial, double2* out, cudaStream_t st) {
+  const unsigned nb = nblk(n);
+  k_dot_partial<<<dim3(nb, nvec), kVT, 0, st>>>(a, b, n, stride, partial);
+  k_finish2<<<nvec, kVT, 0, st>>>(partial, (int)nb, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_norm2(const double2* a, long long n, int nvec, long long stride, double* partial, double* out,
+                         cudaStream_t st) {
+  const unsigned nb = nblk(n);
+  k_norm2_partial<<<dim3(nb, nvec), kVT, 0, st>>>(a, n, stride, partial);
+  k_finish1<<<nvec, kVT, 0, st>>>(partial, (int)nb, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_axpy_dot(double2* y, const double2* x, const double2* coef, const double2* z, long long n,
+                            int nvec, long long stride, double2* partial, double2* dotout, int conj_first_y,
+                            cudaStream_t st) {
+  const unsigned nb = nblk(n);
+  k_axpy_dot<<<dim3(nb, nvec), kVT, 0, st>>>(y, x, coef, z, n, stride, dotout ? partial : nullptr, conj_first_y);
+  if (dotout) k_finish2<<<nvec, kVT, 0, st>>>(partial, (int)nb, dotout);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scale(double2* y, const double2* x, const double2* coef, int invert, long long n, int nvec,
+                         long long stride, cudaStream_t st) {
+  k_scale<<<dim3(nblk(n), nvec), kVT, 0, st>>>(y, x, coef, invert, n, stride);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lincomb(double2* y, const double2* basis, long long bsv, long long bsr, const double2* coef,
+                           int ncoef, long long n, int nvec, long long ys, cudaStream_t st) {
+  k_lincomb<<<dim3(nblk(n), nvec), kVT, 0, st>>>(y, basis, bsv, bsr, coef, ncoef, n, ys);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sub(double2* y, const double2* a, const double2* b, long long n, cudaStream_t st) {
+  k_sub<<<nblk(n), kVT, 0, st>>>(y, a, b, n);
+  return cudaGetLastError();
+}
+
+}  // namespace lsw

@@ -1,0 +1,144 @@
+"""GPU parity of the CUDA path (through the C ABI) against the oracle.
+
+Tolerances: FP64 (complex128) factors and applies must match the oracle's
+SuperLU-based restatement to 1e-10 relative (different but exact-arithmetic-
+equivalent factorisations, so only rounding separates them); the complex64
+mixed path to 2e-4 relative on the preconditioner.  Solves: true relative
+residual <= 1e-6 and relative difference <= 1e-5 against the global direct
+solve; reference-mode GMRES iteration count within +-1 of the oracle."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from lsweeps.problems import ProblemSpec, small, config  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
+FIXTURES = sorted(GOLDEN.glob("*.npz"))
+
+
+def _solver(spec, med, prec):
+    from lsweeps.solver import Solver
+    S = Solver(spec, med, precision=prec)
+    S.factorize()
+    return S
+
+
+def _load(f):
+    d = np.load(f)
+    N, m, p = (int(v) for v in d["Nmp"])
+    spec = ProblemSpec(N=N, m=m, p=p, h=float(d["h"]), omega=float(d["omega"]))
+    spec.sources = [tuple(s) for s in d["sources"]]
+    return spec, d
+
+
+def _dev(v):
+    return torch.from_numpy(np.ascontiguousarray(v)).to("cuda")
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("f", FIXTURES, ids=lambda p: p.stem)
+def test_apply_A_matches_oracle(f):
+    spec, d = _load(f)
+    S = _solver(spec, d["m_grid"], "c128")
+    y = S.apply_A(_dev(d["v"])).cpu().numpy()
+    assert rel(y, d["Av"]) <= 1e-13
+
+
+@pytest.mark.parametrize("f", FIXTURES, ids=lambda p: p.stem)
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-10), ("c64", 2e-4)])
+def test_precond_matches_oracle(f, prec, tol):
+    spec, d = _load(f)
+    S = _solver(spec, d["m_grid"], prec)
+    y = S.apply_precond(_dev(d["v"])).cpu().numpy()
+    assert rel(y, d["Mv"]) <= tol
+
+
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-10), ("c64", 2e-4)])
+def test_local_solve_matches_superlu(prec, tol):
+    from oracle.lsweeps_oracle import OracleProblem
+    spec, med = small(N=3, m=12, p=5, medium="layered", seed=2)
+    P = OracleProblem(spec.N, spec.m, spec.p, spec.h, spec.omega, med)
+    S = _solver(spec, med, prec)
+    rng = np.random.default_rng(5)
+    for c in (0, 4, 8):
+        cell = P.dd.cells[c]
+        cell.factorize()
+        n = cell.size
+        b = rng.standard_normal((2, n)) + 1j * rng.standard_normal((2, n))
+        x = S.local_solve(c, _dev(b.ravel())).cpu().numpy().reshape(2, n)
+        for r in range(2):
+            assert rel(x[r], cell.solve(b[r])) <= tol
+
+
+@pytest.mark.parametrize("f", FIXTURES, ids=lambda p: p.stem)
+def test_reference_gmres_iteration_count(f):
+    spec, d = _load(f)
+    S = _solver(spec, d["m_grid"], "c128")
+    x, rep = S.gmres(_dev(d["b"]), mode="reference", tol=1e-6, max_iter=40)
+    assert abs(rep.iterations - int(d["gmres_ref_iters"])) <= 1
+    n = min(len(rep.log), len(d["gmres_ref_log"]))
+    assert np.allclose(rep.log[:n], d["gmres_ref_log"][:n], rtol=1e-6, atol=1e-12)
+    if rep.iterations == int(d["gmres_ref_iters"]):
+        assert rel(x.cpu().numpy(), d["gmres_ref_x"]) <= 1e-8
+
+
+@pytest.mark.parametrize("f", FIXTURES, ids=lambda p: p.stem)
+@pytest.mark.parametrize("prec", ["c128", "c64"])
+def test_fgmres_solves_to_tolerance(f, prec):
+    spec, d = _load(f)
+    S = _solver(spec, d["m_grid"], prec)
+    x, rep = S.gmres(_dev(d["b"]), mode="flexible", tol=1e-6, max_iter=100, restart=30)
+    assert rep.converged and rep.true_rel_res <= 1e-6
+    assert rel(x.cpu().numpy(), d["x_direct"]) <= 1e-5
+
+
+def test_batched_rhs_equal_single():
+    f = FIXTURES[-1]
+    spec, d = _load(f)
+    for prec in ("c128", "c64"):
+        S = _solver(spec, d["m_grid"], prec)
+        rng = np.random.default_rng(9)
+        V = rng.standard_normal((3, S.n2)) + 1j * rng.standard_normal((3, S.n2))
+        Y = S.apply_precond(_dev(V.ravel())).cpu().numpy().reshape(3, -1)
+        for r in range(3):
+            y = S.apply_precond(_dev(V[r])).cpu().numpy()
+            assert np.array_equal(y, Y[r])
+
+
+def test_c1_precond_and_solve_match_oracle():
+    """Configuration C1 (4x4 cells of 64^2, PML 10, c = 1, 10 ppw) in FP64."""
+    import scipy.sparse.linalg as spla
+    from oracle.lsweeps_oracle import OracleProblem
+    spec, med = config("C1")
+    P = OracleProblem(spec.N, spec.m, spec.p, spec.h, spec.omega, med)
+    P.dd.factorize()
+    S = _solver(spec, med, "c128")
+    rng = np.random.default_rng(11)
+    v = rng.standard_normal(S.n2) + 1j * rng.standard_normal(S.n2)
+    assert rel(S.apply_precond(_dev(v)).cpu().numpy(), P.apply_precond_global(v)) <= 1e-10
+    b = S.assemble_rhs(spec.sources)
+    bo = P.global_rhs(spec.sources)
+    assert rel(b.cpu().numpy(), bo) <= 1e-12
+    x, rep = S.gmres(b, mode="flexible", tol=1e-6, max_iter=100, restart=20)
+    xd = spla.splu(P.global_matrix().tocsc()).solve(bo)
+    assert rep.true_rel_res <= 1e-6 and rel(x.cpu().numpy(), xd) <= 1e-5
+
+
+def test_error_paths():
+    from lsweeps import capi
+    from lsweeps.solver import Solver
+    spec, med = small(N=2, m=10, p=4)
+    S = Solver(spec, med, precision="c64")
+    v = torch.zeros(S.n2, dtype=torch.complex128, device="cuda")
+    with pytest.raises(capi.LswError) as e:
+        S.apply_precond(v)
+    assert e.value.status == 5   # LSW_ERR_NOT_FACTORIZED
+    with pytest.raises(ValueError):
+        Solver(spec, med[:-1], precision="c64")
