@@ -1,0 +1,381 @@
+"""Benchmark of the GB300 L-sweeps path: FGMRES + checkerboard L-sweep
+preconditioner solves of configuration C2 (1031^2 elements, Gaussian-lens
+medium, 8 x 8 cells of 128^2, PML 16, 8 points per wavelength at c_min).
+
+A step is one complete solve to true relative residual 1e-6 with the cell
+factors resident in HBM (complex64 factors and applies inside FP64 flexible
+GMRES(30)); the plain FP64 GPU path (complex128 factors) is measured beside it.
+Prints one JSON line (see the keys below).  `--impl reference` times the CPU
+oracle's restatement of the reference instead (the reference itself cannot be
+built: no Eigen / libconfig++ / MPI)."""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+for _p in (ROOT, ROOT / "l-sweeps-2d_gb300"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+METRIC = "time-to-solution & solves/s at rel. residual 1e-6: mixed vs FP64 on GB300; p50/p99"
+UNIT = "solves/s"
+WORKLOAD = ("C2: 2D Helmholtz, 1031^2 elements (1062^2 DOFs with PML), Gaussian lens c=1-0.4exp(-r^2/0.02), "
+            "8 ppw at c_min, 8x8 checkerboard of 128^2 cells, PML 16, 1 point source, FGMRES(30) tol 1e-6")
+
+
+def pctl(v, q):
+    s = sorted(v)
+    if not s:
+        return None
+    k = (len(s) - 1) * q
+    f = int(k)
+    c = min(f + 1, len(s) - 1)
+    return s[f] + (s[c] - s[f]) * (k - f)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self):
+        if self.p is None:
+            return None
+        self.f.flush()
+        rows = [r.split(",") for r in Path(self.f.name).read_text().strip().splitlines() if r.strip()]
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs"), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle (SuperLU local solves) on a bounded sample
+# ---------------------------------------------------------------------------
+def cpu_sample(spec, med, iterations: int, budget_s: float = 25.0) -> dict:
+    """Time the oracle's cell solves (SuperLU, one thread) on a sample of the
+    C2 cells and extrapolate to one preconditioner apply (the apply is a sum of
+    cell solves: N^2 + 4N(N-1) + 4(N-1)^2 per shifted decomposition, x4) and
+    to one solve of `iterations` FGMRES iterations (iterations + 1 applies)."""
+    import numpy as np
+    from oracle.lsweeps_oracle import AssemblerHelmholtz2DFD, SubdomainStructured, grid_medium
+    t0 = time.perf_counter()
+    # one interior cell of C2 (column/row 1): interior domain [a - 2h, b + 4h],
+    # (m + 6 + 2p - 1)^2 DOFs, assembled and factorised by the oracle
+    h, m = spec.h, spec.m
+    a = (m + 1) * h
+    dom = ((a - 2 * h, a + m * h + 4 * h), (a - 2 * h, a + m * h + 4 * h))
+    asm = AssemblerHelmholtz2DFD(spec.omega, spec.p * h, grid_medium(med, h, spec.p))
+    asm.set_domain(dom)
+    asm.set_n((m + 6, m + 6))
+    cell = SubdomainStructured(asm, 1, 1)
+    cell.A = asm.assemble_system_matrix()
+    cell.size = cell.A.shape[0]
+    setup_s = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    cell.factorize()
+    fact_s = time.perf_counter() - t1
+    rng = np.random.default_rng(0)
+    n = cell.size
+    ts, k = [], 0
+    t2 = time.perf_counter()
+    while time.perf_counter() - t2 < budget_s and k < 400:
+        b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        t = time.perf_counter()
+        cell.solve(b)
+        ts.append(time.perf_counter() - t)
+        k += 1
+    t_solve = statistics.median(ts)
+    N = spec.N
+    n_solves = 4 * (N * N + 4 * N * (N - 1) + 4 * (N - 1) ** 2)
+    t_apply = n_solves * t_solve
+    t_sol = (iterations + 1) * t_apply
+    return {
+        "value": 1.0 / t_sol, "unit": UNIT, "cores": 1, "kind": "port",
+        "sample": (f"oracle (numpy/SciPy SuperLU, 1 thread): {k} solves of one interior C2-shaped cell "
+                   f"({n} DOFs, median {t_solve * 1e3:.2f} ms) x {n_solves} cell solves per apply x "
+                   f"{iterations + 1} applies per solve; cell factorisation {fact_s:.2f} s x {N * N} cells "
+                   f"not included (factors resident on both sides)"),
+        "t_apply_s": t_apply, "t_solve_s": t_sol, "cell_factorize_s": fact_s, "setup_s": setup_s,
+    }
+
+
+def run_reference(args):
+    """--impl reference: the CPU restatement of the reference path, timed on
+    the host cores; rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from lsweeps.problems import config
+    spec, med = config("C2")
+    its = args.ref_iterations
+    samples = []
+    for _ in range(max(1, args.warmup)):
+        cpu_sample(spec, med, its, budget_s=2.0)
+    for _ in range(args.steps):
+        samples.append(cpu_sample(spec, med, its, budget_s=args.ref_budget))
+    vals = [s["value"] for s in samples]
+    v = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "iterations_assumed": its},
+        "cpu_baseline": {k: samples[-1][k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import numpy as np
+    import torch
+    from lsweeps.problems import config
+    from lsweeps.solver import Solver
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    spec, med = config("C2")
+    S = Solver(spec, med, precision="c64", device=local)
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    S.factorize()
+    e1.record(st)
+    torch.cuda.synchronize()
+    fact_s = e0.elapsed_time(e1) / 1e3
+    b = S.assemble_rhs(spec.sources)
+    x = torch.empty_like(b)
+
+    def solve():
+        return S.gmres(b, mode="flexible", tol=args.tol, max_iter=300, restart=30, x=x)
+
+    for _ in range(args.warmup):
+        _, rep = solve()
+    launches0 = S.info()["kernel_launches"]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    reps = []
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            ev[i][0].record(st)
+            _, rep = solve()
+            ev[i][1].record(st)
+            reps.append(rep)
+        torch.cuda.synchronize()
+        elapsed = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    gpu_launches = S.info()["kernel_launches"] - launches0
+    step_ms = [a.elapsed_time(c) for a, c in ev]
+    dev_total = sum(step_ms) / 1e3
+    if dist:
+        t = torch.tensor([dev_total], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_total = float(t.item())
+    value = world * args.steps / dev_total
+
+    # roofline of the dominant kernel (sweep fronts) from CUDA events
+    prof_runs = []
+    v = torch.randn(S.n2, dtype=torch.complex128, device=dev)
+    for _ in range(3):
+        _, pr = S.apply_precond_profiled(v)
+        prof_runs.append(pr)
+    front_ms = statistics.median(p["front_ms"] for p in prof_runs)
+    pr = prof_runs[-1]
+    peak, peak_kind = measured_peaks()
+    achieved = pr["alg_bytes"] / (front_ms / 1e3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "front_kernel_traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get("bytes_per_apply_c2")
+        except Exception:
+            traffic = None
+
+    # end to end through the host-buffer C call (H2D of b, D2H of x in the timed region)
+    bh = torch.empty(S.n2, dtype=torch.complex128, pin_memory=True)
+    bh.copy_(b.cpu())
+    bnp = bh.numpy()
+    for _ in range(1):
+        S.solve_host(bnp, tol=args.tol, max_iter=300, restart=30)
+    torch.cuda.synchronize()
+    te = []
+    for _ in range(args.e2e_steps):
+        t = time.perf_counter()
+        xh, rep_h = S.solve_host(bnp, tol=args.tol, max_iter=300, restart=30)
+        te.append(time.perf_counter() - t)
+    e2e_value = world * len(te) / sum(te)
+
+    # plain FP64 GPU path
+    S64 = None
+    fp64 = None
+    if args.fp64_steps > 0:
+        S64 = Solver(spec, med, precision="c128", device=local)
+        e0.record(st)
+        S64.factorize()
+        e1.record(st)
+        torch.cuda.synchronize()
+        f64_fact = e0.elapsed_time(e1) / 1e3
+        x64 = torch.empty_like(b)
+        S64.gmres(b, mode="flexible", tol=args.tol, max_iter=300, restart=30, x=x64)
+        t64, r64 = [], None
+        for _ in range(args.fp64_steps):
+            a1, a2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a1.record(st)
+            _, r64 = S64.gmres(b, mode="flexible", tol=args.tol, max_iter=300, restart=30, x=x64)
+            a2.record(st)
+            torch.cuda.synchronize()
+            t64.append(a1.elapsed_time(a2))
+        fp64 = {"p50_ms": pctl(t64, 0.5), "p99_ms": pctl(t64, 0.99), "iterations": r64.iterations,
+                "true_rel_res": r64.true_rel_res, "factorize_s": f64_fact, "steps": len(t64)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_sample(spec, med, reps[-1].iterations, budget_s=args.ref_budget)
+        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    clocks = clk.summary()
+    if rank == 0:
+        p50 = pctl(step_ms, 0.5)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_total * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64 factors/applies + f64 Krylov",
+            "data": "synthetic (seeded Gaussian-lens medium)",
+            "config": {"workload": WORKLOAD, "precision": "mixed", "restart": 30, "tol": args.tol,
+                       "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2: 2.3 GB of c64 factors streamed per apply (L2 129 MB)"},
+            "p50_ms": p50, "p99_ms": pctl(step_ms, 0.99), "iterations": reps[-1].iterations,
+            "true_rel_res": reps[-1].true_rel_res, "factorize_s": fact_s,
+            "time_to_solution_s": fact_s + p50 / 1e3,
+            "fp64": fp64,
+            "mixed_vs_fp64_speedup": (fp64["p50_ms"] / p50) if fp64 else None,
+            "mixed_vs_fp64_tts_speedup": ((fp64["factorize_s"] + fp64["p50_ms"] / 1e3) / (fact_s + p50 / 1e3))
+            if fp64 else None,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak if peak else None, "traffic": traffic,
+                         "kernel": "k_front (sweep-front cell solves), all fronts of one apply",
+                         "peak_kind": peak_kind, "alg_bytes_per_apply": pr["alg_bytes"],
+                         "front_ms_per_apply": front_ms, "fronts": pr["fronts"], "items": pr["items"],
+                         "slots": pr["slots"], "apply_ms": pr["total_ms"]},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": S.n2 * 16,
+                    "d2h_bytes_per_step": S.n2 * 16, "steps": len(te)},
+            "clocks": clocks,
+            "gpu_launches": gpu_launches,
+            "wall_s_timed": elapsed,
+        }
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_apply_only(args):
+    """Set up and factorise one configuration, then run `--warmup` + `--steps`
+    preconditioner applies on a random vector (the workload of the ncu captures)."""
+    import torch
+    from lsweeps.problems import config
+    from lsweeps.solver import Solver
+    spec, med = config(args.config)
+    S = Solver(spec, med, precision=args.precision)
+    S.factorize()
+    v = torch.randn(S.n2 * args.nrhs, dtype=torch.complex128, device="cuda")
+    for _ in range(args.warmup + args.steps):
+        S.apply_precond(v)
+    torch.cuda.synchronize()
+    print(json.dumps({"apply_only": args.config, "precision": args.precision, "nrhs": args.nrhs,
+                      "applies": args.warmup + args.steps, "fronts_per_apply": 3 * spec.N - 3 + 1}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--tol", type=float, default=1e-6)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ref-budget", type=float, default=15.0)
+    ap.add_argument("--ref-iterations", type=int, default=14)
+    ap.add_argument("--apply-only", action="store_true", help="only preconditioner applies (profiling workload)")
+    ap.add_argument("--config", default="C2")
+    ap.add_argument("--precision", default="c64")
+    ap.add_argument("--nrhs", type=int, default=1)
+    args = ap.parse_args()
+    if args.apply_only:
+        run_apply_only(args)
+    elif args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

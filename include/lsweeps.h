@@ -88,7 +88,21 @@ typedef struct lsw_problem_info {
   long long device_bytes;  /* all device memory held by the problem */
   double omega;
   double pml_C;       /* PML absorption C = ln(omega) (Input.cpp:836) */
+  long long kernel_launches; /* kernels launched by this context so far */
 } lsw_problem_info;
+
+/* Per-apply measurement of the sweep-front kernels (CUDA events around each
+ * front launch on the caller's stream). */
+typedef struct lsw_apply_profile {
+  int fronts;            /* front launches per apply */
+  int items;             /* cell solves (CTAs) per apply */
+  int slots;             /* right-hand sides over all cell solves */
+  double front_ms;       /* summed device time of the front kernels */
+  double total_ms;       /* device time of the whole apply */
+  double alg_bytes;      /* algorithmic bytes of the front kernels: per cell solve
+                            2 F + 4 R nx ny s, F = nx ny^2 s the factor, R slots */
+  double alg_flops;      /* 2 x 8 nx ny^2 R real flops per cell solve */
+} lsw_apply_profile;
 
 /* One subdomain (SubdomainStructured) in local DOF coordinates:
  * local DOF (i, j) <-> global DOF (lo_x + i, lo_y + j). */
@@ -152,6 +166,12 @@ lsw_status lsw_factorize(lsw_ctx* ctx, void* stream);
 /* DDCheckerboard::applyPrecond (DDCheckerboard.cpp:687-739): y = M^-1 x for a
  * batch of nrhs global vectors. */
 lsw_status lsw_apply_precond(lsw_ctx* ctx, const void* x_dev, void* y_dev, int nrhs, void* stream);
+
+/* lsw_apply_precond with the front kernels timed by CUDA events; synchronises
+ * the stream.  No counterpart in the reference (its only timers are
+ * gettimeofday around factorize and GMRES, Problem.cpp:101-145). */
+lsw_status lsw_apply_precond_profiled(lsw_ctx* ctx, const void* x_dev, void* y_dev, int nrhs, void* stream,
+                                      lsw_apply_profile* prof);
 
 /* DDCheckerboard::applySystemMatrix (DDCheckerboard.cpp:2611-2635): y = A x,
  * the global 5-point operator, FP64. */

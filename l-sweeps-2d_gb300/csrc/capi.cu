@@ -7,6 +7,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <stdexcept>
@@ -16,7 +17,6 @@
 
 namespace lsw {
 bool factor_needs_work(int max_ny, bool dbl);
-int front_rmax(bool dbl);
 }
 
 using namespace lsw;
@@ -59,6 +59,11 @@ struct lsw_ctx {
   // local-solve workspace
   DevBuf ls_items, ls_slots, ls_scratch;
   size_t fixed_bytes = 0;
+  long long launches = 0;
+  int nsm = 152;
+  int max_cluster = 8;
+  // optional per-front timing of one apply
+  std::vector<cudaEvent_t>* front_events = nullptr;
 };
 
 namespace {
@@ -80,6 +85,12 @@ lsw_status cuda_fail(lsw_ctx* c, cudaError_t e, const char* where) {
   do {                                                      \
     cudaError_t _e = (call);                                \
     if (_e != cudaSuccess) return cuda_fail(ctx, _e, where); \
+  } while (0)
+// CK for a launcher that enqueues n kernels; counts them
+#define KL(n, call, where)      \
+  do {                          \
+    CK(call, where);            \
+    ctx->launches += (n);       \
   } while (0)
 
 inline size_t csize(int prec) { return prec == LSW_PREC_C64 ? 8 : 16; }
@@ -181,13 +192,21 @@ lsw_status precond_impl(lsw_ctx* ctx, const double2* x, double2* y, int nrhs, cu
   a.x_in = x;
   a.x_stride = ctx->n2;
   a.n_dof = ctx->n_dof; a.N = ctx->N; a.m = ctx->m; a.p = ctx->p;
-  for (const Front& f : sc->fronts) {
+  a.err = ctx->d_status.as<int>() + 1;
+  for (size_t fi = 0; fi < sc->fronts.size(); ++fi) {
+    const Front& f = sc->fronts[fi];
     a.items = sc->d_items + f.item_begin;
     a.item_count = f.item_count;
+    a.max_slots = f.max_slots;
+    a.cluster = std::min(ctx->max_cluster, front_cluster(f.item_count, ctx->nsm));
+    if (ctx->front_events) CK(cudaEventRecord((*ctx->front_events)[2 * fi], st), "event");
     cudaError_t e = ctx->prec == LSW_PREC_C64 ? launch_front<float>(a, ctx->max_ny, st)
                                               : launch_front<double>(a, ctx->max_ny, st);
     CK(e, "front kernel");
+    if (ctx->front_events) CK(cudaEventRecord((*ctx->front_events)[2 * fi + 1], st), "event");
+    ctx->launches += f.item_count > 0 ? 1 : 0;
   }
+  ctx->launches += 1;
   cudaError_t e = ctx->prec == LSW_PREC_C64 ? launch_combine<float>(ctx->d_outs.p, y, nrhs, ctx->n2, st)
                                             : launch_combine<double>(ctx->d_outs.p, y, nrhs, ctx->n2, st);
   CK(e, "combine kernel");
@@ -197,6 +216,17 @@ lsw_status precond_impl(lsw_ctx* ctx, const double2* x, double2* y, int nrhs, cu
 lsw_status apply_A_impl(lsw_ctx* ctx, const double2* x, double2* y, int nrhs, cudaStream_t st) {
   CK(launch_apply_A(x, y, nrhs, ctx->n_dof, ctx->d_gprof.as<double2>(), ctx->d_m.as<double>(),
                     ctx->omega * ctx->omega, st), "apply_A kernel");
+  ctx->launches += 1;
+  return LSW_OK;
+}
+
+// reads the sweep kernels' error word (synchronises the stream)
+lsw_status check_kernel_err(lsw_ctx* ctx, cudaStream_t st) {
+  int e = 0;
+  CK(cudaMemcpyAsync(&e, ctx->d_status.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H err");
+  CK(cudaStreamSynchronize(st), "sync");
+  if (e & 4) return fail(ctx, LSW_ERR_CUDA, "sweep-front launch did not form the requested clusters (results invalid)");
+  if (e) return fail(ctx, LSW_ERR_CUDA, "a sweep-front kernel gave up on a bounded wait (results invalid)");
   return LSW_OK;
 }
 
@@ -266,6 +296,13 @@ lsw_status lsw_ctx_create(lsw_ctx** out, int device) {
   if (e != cudaSuccess) return LSW_ERR_CUDA;
   lsw_ctx* c = new lsw_ctx;
   c->device = device;
+  int nsm = 0;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) == cudaSuccess && nsm > 0) c->nsm = nsm;
+  // LSW_MAX_CLUSTER caps the CTAs per cell solve (1, 2, 4 or 8; default 8)
+  if (const char* ev = std::getenv("LSW_MAX_CLUSTER")) {
+    const int v = std::atoi(ev);
+    if (v >= 1 && v <= 8) c->max_cluster = v;
+  }
   *out = c;
   return LSW_OK;
 }
@@ -356,6 +393,7 @@ lsw_status lsw_problem_info_get(const lsw_ctx* ctx, lsw_problem_info* o) {
   o->factor_bytes = (long long)ctx->d_fac.bytes;
   o->device_bytes = (long long)device_bytes(ctx);
   o->omega = ctx->omega; o->pml_C = ctx->C;
+  o->kernel_launches = ctx->launches;
   return LSW_OK;
 }
 
@@ -374,6 +412,7 @@ lsw_status lsw_factorize(lsw_ctx* ctx, void* stream) {
   CK(cudaSetDevice(ctx->device), "cudaSetDevice");
   cudaStream_t st = S(stream);
   CK(cudaMemsetAsync(ctx->d_status.p, 0, 16, st), "memset status");
+  ctx->launches += 1;
   const double w2 = ctx->omega * ctx->omega;
   cudaError_t e = ctx->prec == LSW_PREC_C64
                       ? launch_factorize<float>(ctx->d_cells.as<DevCell>(), ctx->ncell, ctx->d_prof.as<double2>(),
@@ -399,6 +438,58 @@ lsw_status lsw_apply_precond(lsw_ctx* ctx, const void* x, void* y, int nrhs, voi
   return precond_impl(ctx, reinterpret_cast<const double2*>(x), reinterpret_cast<double2*>(y), nrhs, S(stream));
 }
 
+lsw_status lsw_apply_precond_profiled(lsw_ctx* ctx, const void* x, void* y, int nrhs, void* stream,
+                                      lsw_apply_profile* prof) {
+  if (!ctx || !x || !y || nrhs < 1 || !prof) return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "bad arguments");
+  if (!ctx->is_setup) return fail(ctx, LSW_ERR_NOT_SET_UP, "lsw_problem_setup first");
+  if (!ctx->factorized) return fail(ctx, LSW_ERR_NOT_FACTORIZED, "lsw_factorize first");
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  cudaStream_t st = S(stream);
+  Schedule* sc = nullptr;
+  lsw_status s = ensure_batch(ctx, nrhs, &sc);
+  if (s != LSW_OK) return s;
+  std::vector<cudaEvent_t> ev(2 * sc->fronts.size() + 2);
+  for (auto& e : ev) CK(cudaEventCreate(&e), "cudaEventCreate");
+  ctx->front_events = &ev;
+  CK(cudaEventRecord(ev[ev.size() - 2], st), "event");
+  s = precond_impl(ctx, reinterpret_cast<const double2*>(x), reinterpret_cast<double2*>(y), nrhs, st);
+  ctx->front_events = nullptr;
+  if (s != LSW_OK) { for (auto& e : ev) cudaEventDestroy(e); return s; }
+  CK(cudaEventRecord(ev[ev.size() - 1], st), "event");
+  CK(cudaEventSynchronize(ev[ev.size() - 1]), "event sync");
+  if ((s = check_kernel_err(ctx, st)) != LSW_OK) return s;
+  double fm = 0.0;
+  for (size_t f = 0; f < sc->fronts.size(); ++f) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ev[2 * f], ev[2 * f + 1]), "elapsed");
+    fm += ms;
+  }
+  float tot = 0.f;
+  CK(cudaEventElapsedTime(&tot, ev[ev.size() - 2], ev[ev.size() - 1]), "elapsed");
+  for (auto& e : ev) cudaEventDestroy(e);
+  // algorithmic bytes / flops from the schedule
+  std::vector<DevItem> items(sc->fronts.empty() ? 0 : sc->fronts.back().item_begin + sc->fronts.back().item_count);
+  CK(cudaMemcpy(items.data(), sc->d_items, items.size() * sizeof(DevItem), cudaMemcpyDeviceToHost), "D2H items");
+  const double cs = (double)csize(ctx->prec);
+  double bytes = 0.0, flops = 0.0;
+  int slots = 0;
+  for (const DevItem& it : items) {
+    const DevCell& c = ctx->cells[it.cell];
+    const double F = (double)c.nx * c.ny * c.ny * cs;
+    bytes += 2.0 * F + 4.0 * it.slot_count * (double)c.nx * c.ny * cs;
+    flops += 2.0 * 8.0 * (double)c.nx * c.ny * c.ny * it.slot_count;
+    slots += it.slot_count;
+  }
+  prof->fronts = (int)sc->fronts.size();
+  prof->items = (int)items.size();
+  prof->slots = slots;
+  prof->front_ms = fm;
+  prof->total_ms = tot;
+  prof->alg_bytes = bytes;
+  prof->alg_flops = flops;
+  return LSW_OK;
+}
+
 lsw_status lsw_apply_A(lsw_ctx* ctx, const void* x, void* y, int nrhs, void* stream) {
   if (!ctx || !x || !y || nrhs < 1) return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "bad arguments to lsw_apply_A");
   if (!ctx->is_setup) return fail(ctx, LSW_ERR_NOT_SET_UP, "lsw_problem_setup first");
@@ -417,7 +508,7 @@ lsw_status lsw_assemble_rhs(lsw_ctx* ctx, const double* src, const double* amp, 
   CK(ctx->k_small2.ensure(hs.size() * sizeof(double) + 64), "cudaMalloc(src)");
   CK(cudaMemcpyAsync(ctx->k_small2.p, hs.data(), hs.size() * sizeof(double), cudaMemcpyHostToDevice, st), "H2D src");
   // eps = DD mesh size (Input.cpp:243): every cell has mesh size h on the integer grid
-  CK(launch_rhs(reinterpret_cast<double2*>(b), ctx->n_dof, ctx->p, ctx->h, ctx->k_small2.as<double>(),
+  KL(1, launch_rhs(reinterpret_cast<double2*>(b), ctx->n_dof, ctx->p, ctx->h, ctx->k_small2.as<double>(),
                 ctx->k_small2.as<double>() + 2 * nsrc, nsrc, ctx->h, st), "rhs kernel");
   CK(cudaStreamSynchronize(st), "rhs sync");
   return LSW_OK;
@@ -442,7 +533,7 @@ lsw_status lsw_local_solve(lsw_ctx* ctx, int cell, const void* b, void* x, int n
     it.cell = cell; it.slot_begin = (int)slots.size(); it.group_begin = 0; it.group_count = 0;
     it.slot_count = std::min(rmax, nrhs - r0);
     it.scratch_off = scr;
-    scr += (long long)cl.nx * it.slot_count * cl.ldn;
+    scr += (long long)cl.nx * front_rpad(it.slot_count) * cl.ny;
     for (int r = r0; r < r0 + it.slot_count; ++r) {
       DevSlot s{};
       s.kind = SK_CELLVEC; s.rhs = r;
@@ -471,10 +562,13 @@ lsw_status lsw_local_solve(lsw_ctx* ctx, int cell, const void* b, void* x, int n
   a.out_stride = (long long)cl.nx * cl.ny;
   a.n_dof = ctx->n_dof; a.N = ctx->N; a.m = ctx->m; a.p = ctx->p;
   a.item_count = (int)items.size();
+  a.max_slots = std::min(rmax, nrhs);
+  a.err = ctx->d_status.as<int>() + 1;
+  a.cluster = std::min(ctx->max_cluster, front_cluster(a.item_count, ctx->nsm));
   cudaError_t e = dbl ? launch_front<double>(a, ctx->max_ny, st) : launch_front<float>(a, ctx->max_ny, st);
   CK(e, "local solve kernel");
-  CK(cudaStreamSynchronize(st), "local solve sync");
-  return LSW_OK;
+  ctx->launches += 1;
+  return check_kernel_err(ctx, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -510,9 +604,9 @@ static lsw_status gmres_reference(lsw_ctx* ctx, const double2* b, double2* x, in
   if ((s = apply_A_impl(ctx, x, tmp, nv, st)) != LSW_OK) return s;
   if ((s = precond_impl(ctx, tmp, Qi(0), nv, st)) != LSW_OK) return s;
   ++applies;
-  for (int v = 0; v < nv; ++v) CK(launch_sub(Qi(0) + v * n2, rp + v * n2, Qi(0) + v * n2, n2, st), "sub");
-  CK(launch_norm2(rp, n2, nv, n2, reinterpret_cast<double*>(part), ndev, st), "norm");
-  CK(launch_norm2(Qi(0), n2, nv, n2, reinterpret_cast<double*>(part), ndev + nv, st), "norm");
+  for (int v = 0; v < nv; ++v) KL(1, launch_sub(Qi(0) + v * n2, rp + v * n2, Qi(0) + v * n2, n2, st), "sub");
+  KL(2, launch_norm2(rp, n2, nv, n2, reinterpret_cast<double*>(part), ndev, st), "norm");
+  KL(2, launch_norm2(Qi(0), n2, nv, n2, reinterpret_cast<double*>(part), ndev + nv, st), "norm");
   std::vector<double> hn(2 * nv);
   CK(cudaMemcpyAsync(hn.data(), ndev, 2 * nv * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H norms");
   CK(cudaStreamSynchronize(st), "sync");
@@ -533,7 +627,7 @@ static lsw_status gmres_reference(lsw_ctx* ctx, const double2* b, double2* x, in
     std::vector<double2> rsc(nv);
     for (int v = 0; v < nv; ++v) rsc[v] = make_double2(r_norm[v], 0.0);
     CK(cudaMemcpyAsync(cdev, rsc.data(), nv * sizeof(double2), cudaMemcpyHostToDevice, st), "H2D");
-    CK(launch_scale(Qi(0), Qi(0), cdev, 1, n2, nv, n2, st), "scale");
+    KL(1, launch_scale(Qi(0), Qi(0), cdev, 1, n2, nv, n2, st), "scale");
     for (int v = 0; v < nv; ++v) beta[v].push_back(cplx(r_norm[v], 0.0));
     for (int k = 0; k < maxit; ++k) {
       // arnoldi (238-310): q = M^-1 A Q_k ; h_i = q.dot(Q_i) = sum conj(q) Q_i ; q -= h_i Q_i
@@ -541,14 +635,14 @@ static lsw_status gmres_reference(lsw_ctx* ctx, const double2* b, double2* x, in
       double2* q = Qi(k + 1);
       if ((s = precond_impl(ctx, tmp, q, nv, st)) != LSW_OK) return s;
       ++applies;
-      CK(launch_dot(q, Qi(0), n2, nv, n2, part, hdev, st), "dot");
+      KL(2, launch_dot(q, Qi(0), n2, nv, n2, part, hdev, st), "dot");
       for (int i = 0; i <= k; ++i) {
         // coefficients for all rhs of column i sit at hdev[i*nv + v]
         if (i < k)
-          CK(launch_axpy_dot(q, Qi(i), hdev + (size_t)i * nv, Qi(i + 1), n2, nv, n2, part,
+          KL(2, launch_axpy_dot(q, Qi(i), hdev + (size_t)i * nv, Qi(i + 1), n2, nv, n2, part,
                              hdev + (size_t)(i + 1) * nv, 1, st), "axpy_dot");
         else
-          CK(launch_axpy_dot(q, Qi(i), hdev + (size_t)i * nv, nullptr, n2, nv, n2, part,
+          KL(2, launch_axpy_dot(q, Qi(i), hdev + (size_t)i * nv, nullptr, n2, nv, n2, part,
                              hdev + (size_t)(k + 1) * nv, 1, st), "axpy_norm");
       }
       std::vector<double2> hh((size_t)(k + 2) * nv);
@@ -587,7 +681,7 @@ static lsw_status gmres_reference(lsw_ctx* ctx, const double2* b, double2* x, in
       }
       if (o->verbose) printf("iteration %d: %.6e\n", k + 1, logs[0].back());
       CK(cudaMemcpyAsync(cdev, sc.data(), nv * sizeof(double2), cudaMemcpyHostToDevice, st), "H2D");
-      CK(launch_scale(q, q, cdev, 1, n2, nv, n2, st), "scale");
+      KL(1, launch_scale(q, q, cdev, 1, n2, nv, n2, st), "scale");
       kmax = k;
       if (std::all_of(done.begin(), done.end(), [](int d) { return d != 0; })) break;
     }
@@ -609,7 +703,7 @@ static lsw_status gmres_reference(lsw_ctx* ctx, const double2* b, double2* x, in
     CK(ctx->k_small2.ensure(coef.size() * sizeof(double2) + 64), "cudaMalloc(coef)");
     cdev = ctx->k_small2.as<double2>();
     CK(cudaMemcpyAsync(cdev, coef.data(), coef.size() * sizeof(double2), cudaMemcpyHostToDevice, st), "H2D y");
-    CK(launch_lincomb(x, Q, (long long)nv * n2, n2, cdev, ncol, n2, nv, n2, st), "lincomb");
+    KL(1, launch_lincomb(x, Q, (long long)nv * n2, n2, cdev, ncol, n2, nv, n2, st), "lincomb");
   }
   int iters = 0;
   double fl = 0.0;
@@ -654,7 +748,7 @@ static lsw_status gmres_flexible(lsw_ctx* ctx, const double2* b, double2* x, int
   lsw_status s;
   int applies = 0, it = 0;
   CK(cudaMemsetAsync(x, 0, vb, st), "x0 = 0");
-  CK(launch_norm2(b, n2, nv, n2, reinterpret_cast<double*>(part), ndev, st), "norm b");
+  KL(2, launch_norm2(b, n2, nv, n2, reinterpret_cast<double*>(part), ndev, st), "norm b");
   std::vector<double> bn(nv);
   CK(cudaMemcpyAsync(bn.data(), ndev, nv * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
   CK(cudaStreamSynchronize(st), "sync");
@@ -664,8 +758,8 @@ static lsw_status gmres_flexible(lsw_ctx* ctx, const double2* b, double2* x, int
   while (true) {
     // r = b - A x
     if ((s = apply_A_impl(ctx, x, tmp, nv, st)) != LSW_OK) return s;
-    for (int v = 0; v < nv; ++v) CK(launch_sub(Vi(0) + v * n2, b + v * n2, tmp + v * n2, n2, st), "sub");
-    CK(launch_norm2(Vi(0), n2, nv, n2, reinterpret_cast<double*>(part), ndev, st), "norm r");
+    for (int v = 0; v < nv; ++v) KL(1, launch_sub(Vi(0) + v * n2, b + v * n2, tmp + v * n2, n2, st), "sub");
+    KL(2, launch_norm2(Vi(0), n2, nv, n2, reinterpret_cast<double*>(part), ndev, st), "norm r");
     std::vector<double> rn(nv);
     CK(cudaMemcpyAsync(rn.data(), ndev, nv * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
     CK(cudaStreamSynchronize(st), "sync");
@@ -680,7 +774,7 @@ static lsw_status gmres_flexible(lsw_ctx* ctx, const double2* b, double2* x, int
     if (o->verbose) printf("fgmres it %d: true rel. residual %.6e\n", it, rel[0]);
     if (std::all_of(conv.begin(), conv.end(), [](int c) { return c != 0; }) || it >= o->max_iter) break;
     CK(cudaMemcpyAsync(cdev, sc.data(), nv * sizeof(double2), cudaMemcpyHostToDevice, st), "H2D");
-    CK(launch_scale(Vi(0), Vi(0), cdev, 1, n2, nv, n2, st), "scale");
+    KL(1, launch_scale(Vi(0), Vi(0), cdev, 1, n2, nv, n2, st), "scale");
     std::vector<std::vector<cplx>> H(nv, std::vector<cplx>((size_t)(m + 1) * m)), g(nv, std::vector<cplx>(m + 1));
     std::vector<std::vector<cplx>> cs(nv, std::vector<cplx>(m)), sn(nv, std::vector<cplx>(m));
     std::vector<int> active(nv);
@@ -692,13 +786,13 @@ static lsw_status gmres_flexible(lsw_ctx* ctx, const double2* b, double2* x, int
       double2* w = Vi(j + 1);
       if ((s = apply_A_impl(ctx, Zi(j), w, nv, st)) != LSW_OK) return s;
       // MGS: h_i = V_i^H w ; w -= h_i V_i
-      CK(launch_dot(Vi(0), w, n2, nv, n2, part, hdev, st), "dot");
+      KL(2, launch_dot(Vi(0), w, n2, nv, n2, part, hdev, st), "dot");
       for (int i = 0; i <= j; ++i) {
         if (i < j)
-          CK(launch_axpy_dot(w, Vi(i), hdev + (size_t)i * nv, Vi(i + 1), n2, nv, n2, part,
+          KL(2, launch_axpy_dot(w, Vi(i), hdev + (size_t)i * nv, Vi(i + 1), n2, nv, n2, part,
                              hdev + (size_t)(i + 1) * nv, 0, st), "axpy_dot");
         else
-          CK(launch_axpy_dot(w, Vi(i), hdev + (size_t)i * nv, nullptr, n2, nv, n2, part,
+          KL(2, launch_axpy_dot(w, Vi(i), hdev + (size_t)i * nv, nullptr, n2, nv, n2, part,
                              hdev + (size_t)(j + 1) * nv, 0, st), "axpy_norm");
       }
       std::vector<double2> hh((size_t)(j + 2) * nv);
@@ -732,7 +826,7 @@ static lsw_status gmres_flexible(lsw_ctx* ctx, const double2* b, double2* x, int
       }
       if (o->verbose) printf("fgmres it %d: estimate %.6e\n", it, log0.back());
       CK(cudaMemcpyAsync(cdev, sc.data(), nv * sizeof(double2), cudaMemcpyHostToDevice, st), "H2D");
-      CK(launch_scale(w, w, cdev, 1, n2, nv, n2, st), "scale");
+      KL(1, launch_scale(w, w, cdev, 1, n2, nv, n2, st), "scale");
       if (all_small || it >= o->max_iter) break;
     }
     // x += Z y  with y from the triangular system R y = g
@@ -750,7 +844,7 @@ static lsw_status gmres_flexible(lsw_ctx* ctx, const double2* b, double2* x, int
     CK(ctx->k_small2.ensure(coef.size() * sizeof(double2) + 64), "cudaMalloc(coef)");
     cdev = ctx->k_small2.as<double2>();
     CK(cudaMemcpyAsync(cdev, coef.data(), coef.size() * sizeof(double2), cudaMemcpyHostToDevice, st), "H2D y");
-    CK(launch_lincomb(x, Z, (long long)nv * n2, n2, cdev, ncol, n2, nv, n2, st), "lincomb");
+    KL(1, launch_lincomb(x, Z, (long long)nv * n2, n2, cdev, ncol, n2, nv, n2, st), "lincomb");
   }
   double worst = 0.0;
   for (int v = 0; v < nv; ++v) worst = std::max(worst, rel[v]);
@@ -776,10 +870,10 @@ static lsw_status true_residual(lsw_ctx* ctx, const double2* b, const double2* x
   double2* r = ctx->k_tmp2.as<double2>();
   lsw_status s = apply_A_impl(ctx, x, r, nv, st);
   if (s != LSW_OK) return s;
-  for (int v = 0; v < nv; ++v) CK(launch_sub(r + v * n2, b + v * n2, r + v * n2, n2, st), "sub");
+  for (int v = 0; v < nv; ++v) KL(1, launch_sub(r + v * n2, b + v * n2, r + v * n2, n2, st), "sub");
   double* nd = ctx->k_nrm.as<double>();
-  CK(launch_norm2(r, n2, nv, n2, reinterpret_cast<double*>(ctx->k_part.p), nd, st), "norm");
-  CK(launch_norm2(b, n2, nv, n2, reinterpret_cast<double*>(ctx->k_part.p), nd + nv, st), "norm");
+  KL(2, launch_norm2(r, n2, nv, n2, reinterpret_cast<double*>(ctx->k_part.p), nd, st), "norm");
+  KL(2, launch_norm2(b, n2, nv, n2, reinterpret_cast<double*>(ctx->k_part.p), nd + nv, st), "norm");
   std::vector<double> h(2 * nv);
   CK(cudaMemcpyAsync(h.data(), nd, 2 * nv * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
   CK(cudaStreamSynchronize(st), "sync");
@@ -806,6 +900,7 @@ lsw_status lsw_gmres(lsw_ctx* ctx, const void* b, void* x, int nrhs, const lsw_g
   if (s != LSW_OK) return s;
   double tr = 0.0;
   if ((s = true_residual(ctx, bb, xx, nrhs, &tr, st)) != LSW_OK) return s;
+  if ((s = check_kernel_err(ctx, st)) != LSW_OK) return s;
   CK(cudaStreamSynchronize(st), "sync");
   const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (rep) { rep->true_rel_res = tr; rep->seconds = secs; }

@@ -45,7 +45,7 @@ bool geom_valid(const lsw_geom* g, std::string* why) {
   if (!(g->h > 0.0) || !std::isfinite(g->h)) { *why = "h must be positive"; return false; }
   int nd = 0;
   for (int J = 0; J < g->n_cells; ++J) nd = std::max(nd, dir_geom(J, g->n_cells, g->n_els_in_cell, g->pml).nd);
-  if (nd > 256) { *why = "cell side exceeds 256 DOFs (m + 6 + 2p - 1 <= 256)"; return false; }
+  if (nd > 224) { *why = "cell side exceeds 224 DOFs (m + 6 + 2p - 1 <= 224)"; return false; }
   return true;
 }
 
@@ -271,7 +271,7 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, int rmax
   // ---- flatten into items (whole (shift, rhs) groups, at most rmax slots) ----
   fronts.clear(); items.clear(); slots.clear(); groups.clear();
   for (auto& f : fr) {
-    Front F{(int)items.size(), 0, 0};
+    Front F{(int)items.size(), 0, 0, 0};
     for (auto& kv : f) {
       const int c = kv.first;
       auto& v = kv.second;
@@ -303,7 +303,8 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, int rmax
         }
         const DevCell& cl = cells[c];
         it.scratch_off = F.scratch_elems;
-        F.scratch_elems += (long long)cl.nx * it.slot_count * cl.ldn;
+        F.scratch_elems += (long long)cl.nx * front_rpad(it.slot_count) * cl.ny;
+        F.max_slots = std::max(F.max_slots, it.slot_count);
         items.push_back(it);
         F.item_count++;
       }

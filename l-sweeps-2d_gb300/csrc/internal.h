@@ -92,6 +92,7 @@ struct DevItem {
 struct Front {
   int item_begin, item_count;
   long long scratch_elems;
+  int max_slots;
 };
 
 struct Schedule {
@@ -135,9 +136,21 @@ struct FrontArgs {
   long long out_stride;
   int n_dof, N, m, p;
   int item_count;
+  int max_slots;          // largest slot count of an item in this launch
+  int* err;               // bit 1: a bounded wait timed out
+  int cluster;            // CTAs per item (thread-block cluster size)
+  int stages;             // shared-memory ring depth (set by the launcher)
 };
+// CTAs per item for a front of `items` cell solves on `nsm` SMs
+inline int front_cluster(int items, int nsm) {
+  int cl = 8;
+  while (cl > 1 && items * cl > nsm) cl >>= 1;
+  return cl;
+}
 
 template <typename T> cudaError_t launch_front(const FrontArgs& a, int max_ny, cudaStream_t st);
+int front_rmax(bool dbl);
+int front_rpad(int n);
 template <typename T> cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* prof,
                                                    const double* mgrid, int n_dof, double omega2,
                                                    void* fac, void* work, int max_ny, int* status,

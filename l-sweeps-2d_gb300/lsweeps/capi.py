@@ -21,6 +21,7 @@ EXPORTS = [
     "lsw_ctx_create", "lsw_ctx_destroy", "lsw_status_string", "lsw_ctx_last_error", "lsw_geometry_cell",
     "lsw_problem_setup", "lsw_problem_info_get", "lsw_cell_info_get", "lsw_factorize", "lsw_apply_precond",
     "lsw_apply_A", "lsw_assemble_rhs", "lsw_gmres", "lsw_solve_host", "lsw_local_solve",
+    "lsw_apply_precond_profiled",
 ]
 
 
@@ -32,7 +33,13 @@ class Geom(C.Structure):
 class ProblemInfo(C.Structure):
     _fields_ = [("n_g", C.c_int), ("n_dof", C.c_int), ("n_cells_total", C.c_int), ("max_cell_side", C.c_int),
                 ("precision", C.c_int), ("factorized", C.c_int), ("factor_bytes", C.c_longlong),
-                ("device_bytes", C.c_longlong), ("omega", C.c_double), ("pml_C", C.c_double)]
+                ("device_bytes", C.c_longlong), ("omega", C.c_double), ("pml_C", C.c_double),
+                ("kernel_launches", C.c_longlong)]
+
+
+class ApplyProfile(C.Structure):
+    _fields_ = [("fronts", C.c_int), ("items", C.c_int), ("slots", C.c_int), ("front_ms", C.c_double),
+                ("total_ms", C.c_double), ("alg_bytes", C.c_double), ("alg_flops", C.c_double)]
 
 
 class CellInfo(C.Structure):
@@ -92,6 +99,7 @@ def lib() -> C.CDLL:
         "lsw_gmres": (i, [vp, vp, vp, i, C.POINTER(GmresOpts), C.POINTER(GmresReport), vp]),
         "lsw_solve_host": (i, [vp, C.POINTER(d), C.POINTER(d), i, C.POINTER(GmresOpts), C.POINTER(GmresReport), vp]),
         "lsw_local_solve": (i, [vp, i, vp, vp, i, vp]),
+        "lsw_apply_precond_profiled": (i, [vp, vp, vp, i, vp, C.POINTER(ApplyProfile)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -101,6 +101,15 @@ class Solver:
                                             _stream_ptr(stream)), self.ctx)
         return y
 
+    def apply_precond_profiled(self, x, out=None, stream=None) -> tuple:
+        torch = _torch()
+        nr = self._vec(x)
+        y = torch.empty_like(x) if out is None else out
+        prof = capi.ApplyProfile()
+        capi.check(self.L.lsw_apply_precond_profiled(self.ctx, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()),
+                                                     nr, _stream_ptr(stream), C.byref(prof)), self.ctx)
+        return y, {k: getattr(prof, k) for k, _ in capi.ApplyProfile._fields_}
+
     def apply_A(self, x, out=None, stream=None):
         torch = _torch()
         nr = self._vec(x)

@@ -100,16 +100,19 @@ def test_fgmres_solves_to_tolerance(f, prec):
 
 
 def test_batched_rhs_equal_single():
+    """A batch of right-hand sides gives each one's single result; only the
+    summation order inside a cell solve may differ (the number of consumer
+    warps per row group depends on the slots per front)."""
     f = FIXTURES[-1]
     spec, d = _load(f)
-    for prec in ("c128", "c64"):
+    for prec, tol in (("c128", 1e-13), ("c64", 1e-5)):
         S = _solver(spec, d["m_grid"], prec)
         rng = np.random.default_rng(9)
         V = rng.standard_normal((3, S.n2)) + 1j * rng.standard_normal((3, S.n2))
         Y = S.apply_precond(_dev(V.ravel())).cpu().numpy().reshape(3, -1)
         for r in range(3):
             y = S.apply_precond(_dev(V[r])).cpu().numpy()
-            assert np.array_equal(y, Y[r])
+            assert rel(Y[r], y) <= tol
 
 
 def test_c1_precond_and_solve_match_oracle():
