@@ -201,6 +201,26 @@ lsw_status lsw_solve_host(lsw_ctx* ctx, const double* b_host, double* x_host, in
 lsw_status lsw_local_solve(lsw_ctx* ctx, int cell, const void* b_dev, void* x_dev, int nrhs,
                            void* stream);
 
+/* Allocation-free variant of lsw_local_solve.  No counterpart in the reference.
+ * For callers that cannot call cudaMalloc: processes whose device memory is
+ * owned by their own pool under a fixed budget (a serving process that reserves
+ * HBM up front), and latency-bound loops that cannot afford the device-wide
+ * synchronisation an allocation may cause.  The caller passes only inputs and
+ * outputs (same layout as lsw_local_solve); the call allocates nothing.  Its
+ * scratch (descriptors and forward-substitution storage, ~nx*ny*8 bytes per
+ * right-hand side in complex64, twice that in complex128) lives in one fixed
+ * 8 MiB device array inside the library, which every GPU that loads the
+ * library holds until the process exits; a request that does not fit returns
+ * LSW_ERR_INVALID_ARGUMENT with the sizes in lsw_ctx_last_error.
+ * The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (other streams,
+ * other contexts on the same device) race and must be serialised by the
+ * caller.  Nothing in the array needs clearing between calls: every element
+ * is written before it is read. */
+lsw_status lsw_local_solve_noalloc(lsw_ctx* ctx, int cell, const void* b_dev, void* x_dev, int nrhs,
+                                   void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -12,6 +12,7 @@
 #include <map>
 #include <stdexcept>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -271,6 +272,48 @@ struct Krylov {
   lsw_status st_ = LSW_OK;
   double2* part() { return ctx->k_part.as<double2>(); }
 };
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Allocation-free cell solve (lsw_local_solve_noalloc).  Its scratch -- the
+// item/slot descriptors and the forward-substitution storage -- lives in this
+// fixed file-scope device array instead of memory obtained from cudaMalloc.
+// Every GPU that loads the library holds the array until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;   // 8 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// device address of g_noalloc_scratch per device, looked up once per device
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[256] = {};
+
+// writes the descriptors of `nrhs` full-cell right-hand sides of one cell:
+// items of at most rmax slots, each with its share of the forward storage
+__global__ void k_noalloc_desc(DevItem* items, DevSlot* slots, int cell, int nrhs, int rmax,
+                               long long per_item_stride_elems) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrhs) return;
+  const int item = r / rmax;
+  DevSlot s{};
+  s.kind = SK_CELLVEC;
+  s.rhs = r;
+  s.in_lr0 = s.in_lr1 = s.in_ud0 = s.in_ud1 = -1;
+  for (int i = 0; i < 4; ++i) { s.lr_out[i] = -1; s.ud_out[i] = -1; s.lr_line[i] = -1; s.ud_line[i] = -1; }
+  slots[r] = s;
+  if (r % rmax == 0) {
+    DevItem it{};
+    it.cell = cell;
+    it.slot_begin = r;
+    it.slot_count = min(rmax, nrhs - r);
+    it.group_begin = 0;
+    it.group_count = 0;
+    it.scratch_off = (long long)item * per_item_stride_elems;
+    items[item] = it;
+  }
+}
 
 }  // namespace
 
@@ -923,6 +966,72 @@ lsw_status lsw_solve_host(lsw_ctx* ctx, const double* b_host, double* x_host, in
   CK(cudaMemcpyAsync(x_host, dx.p, vb, cudaMemcpyDeviceToHost, st), "D2H x");
   CK(cudaStreamSynchronize(st), "sync");
   return LSW_OK;
+}
+
+lsw_status lsw_local_solve_noalloc(lsw_ctx* ctx, int cell, const void* b, void* x, int nrhs, void* stream) {
+  if (!ctx || !b || !x || nrhs < 1)
+    return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "bad arguments to lsw_local_solve_noalloc");
+  if (!ctx->is_setup) return fail(ctx, LSW_ERR_NOT_SET_UP, "lsw_problem_setup first");
+  if (cell < 0 || cell >= ctx->ncell) return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "cell index out of range");
+  if (!ctx->factorized)
+    return fail(ctx, LSW_ERR_NOT_FACTORIZED, "The linear system has to be factorized before it can be solved");
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  cudaStream_t st = S(stream);
+  const bool dbl = ctx->prec == LSW_PREC_C128;
+  const int rmax = front_rmax(dbl);
+  const DevCell& cl = ctx->cells[cell];
+  const int n_items = (nrhs + rmax - 1) / rmax;
+  const long long per_item = (long long)cl.nx * front_rpad(std::min(rmax, nrhs)) * cl.ny;
+  const size_t desc_bytes = ((size_t)n_items * sizeof(DevItem) + (size_t)nrhs * sizeof(DevSlot) + 255) & ~size_t(255);
+  const size_t need = desc_bytes + (size_t)n_items * per_item * csize(ctx->prec);
+  if (need > kNoAllocScratchBytes) {
+    return fail(ctx, LSW_ERR_INVALID_ARGUMENT,
+                "lsw_local_solve_noalloc: " + std::to_string(nrhs) + " right-hand sides of cell " +
+                    std::to_string(cell) + " need " + std::to_string(need) + " bytes of scratch, more than the " +
+                    std::to_string(kNoAllocScratchBytes) + "-byte fixed buffer; use fewer right-hand sides per call");
+  }
+  // once per device, with that device current: the device address of the array
+  void* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (ctx->device < 0 || ctx->device >= 256) return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "device index out of range");
+    if (!g_noalloc_addr[ctx->device]) {
+      void* p = nullptr;
+      CK(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(no-allocation scratch)");
+      g_noalloc_addr[ctx->device] = p;
+    }
+    base = g_noalloc_addr[ctx->device];
+  }
+  unsigned char* bp = static_cast<unsigned char*>(base);
+  DevItem* d_items = reinterpret_cast<DevItem*>(bp);
+  DevSlot* d_slots = reinterpret_cast<DevSlot*>(bp + (size_t)n_items * sizeof(DevItem));
+  void* d_scr = bp + desc_bytes;
+  // every element of the forward storage is written before it is read, so
+  // nothing in the shared array needs clearing between calls
+  k_noalloc_desc<<<(nrhs + 127) / 128, 128, 0, st>>>(d_items, d_slots, cell, nrhs, rmax, per_item);
+  CK(cudaGetLastError(), "descriptor kernel");
+  FrontArgs a{};
+  a.cells = ctx->d_cells.as<DevCell>();
+  a.items = d_items;
+  a.slots = d_slots;
+  a.groups = nullptr;
+  a.fac = ctx->d_fac.p;
+  a.prof = ctx->d_prof.as<double2>();
+  a.traces = nullptr; a.outs = nullptr;
+  a.scratch = d_scr;
+  a.x_in = reinterpret_cast<const double2*>(b);
+  a.x_stride = (long long)cl.nx * cl.ny;
+  a.x_out = reinterpret_cast<double2*>(x);
+  a.out_stride = (long long)cl.nx * cl.ny;
+  a.n_dof = ctx->n_dof; a.N = ctx->N; a.m = ctx->m; a.p = ctx->p;
+  a.item_count = n_items;
+  a.max_slots = std::min(rmax, nrhs);
+  a.err = ctx->d_status.as<int>() + 1;
+  a.cluster = std::min(ctx->max_cluster, front_cluster(a.item_count, ctx->nsm));
+  cudaError_t e = dbl ? launch_front<double>(a, ctx->max_ny, st) : launch_front<float>(a, ctx->max_ny, st);
+  CK(e, "local solve kernel");
+  ctx->launches += 2;
+  return check_kernel_err(ctx, st);
 }
 
 }  // extern "C"
