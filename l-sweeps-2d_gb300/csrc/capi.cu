@@ -201,8 +201,8 @@ lsw_status precond_impl(lsw_ctx* ctx, const double2* x, double2* y, int nrhs, cu
     a.max_slots = f.max_slots;
     a.cluster = std::min(ctx->max_cluster, front_cluster(f.item_count, ctx->nsm));
     if (ctx->front_events) CK(cudaEventRecord((*ctx->front_events)[2 * fi], st), "event");
-    cudaError_t e = ctx->prec == LSW_PREC_C64 ? launch_front<float>(a, ctx->max_ny, st)
-                                              : launch_front<double>(a, ctx->max_ny, st);
+    cudaError_t e = ctx->prec == LSW_PREC_C64 ? launch_front<float>(a, ctx->max_ny, ctx->max_nx, st)
+                                              : launch_front<double>(a, ctx->max_ny, ctx->max_nx, st);
     CK(e, "front kernel");
     if (ctx->front_events) CK(cudaEventRecord((*ctx->front_events)[2 * fi + 1], st), "event");
     ctx->launches += f.item_count > 0 ? 1 : 0;
@@ -270,7 +270,6 @@ struct Krylov {
   int nv;
   long long n2;
   lsw_status st_ = LSW_OK;
-  double2* part() { return ctx->k_part.as<double2>(); }
 };
 
 }  // namespace
@@ -502,10 +501,16 @@ lsw_status lsw_apply_precond_profiled(lsw_ctx* ctx, const void* x, void* y, int 
   CK(cudaEventSynchronize(ev[ev.size() - 1]), "event sync");
   if ((s = check_kernel_err(ctx, st)) != LSW_OK) return s;
   double fm = 0.0;
+  const bool log_fronts = std::getenv("LSW_FRONT_LOG") != nullptr;   // per-front lines on stderr
   for (size_t f = 0; f < sc->fronts.size(); ++f) {
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, ev[2 * f], ev[2 * f + 1]), "elapsed");
     fm += ms;
+    if (log_fronts) {
+      const Front& fr = sc->fronts[f];
+      std::fprintf(stderr, "front %zu items %d max_slots %d cluster %d ms %.4f\n", f, fr.item_count, fr.max_slots,
+                   std::min(ctx->max_cluster, front_cluster(fr.item_count, ctx->nsm)), ms);
+    }
   }
   float tot = 0.f;
   CK(cudaEventElapsedTime(&tot, ev[ev.size() - 2], ev[ev.size() - 1]), "elapsed");
@@ -608,7 +613,7 @@ lsw_status lsw_local_solve(lsw_ctx* ctx, int cell, const void* b, void* x, int n
   a.max_slots = std::min(rmax, nrhs);
   a.err = ctx->d_status.as<int>() + 1;
   a.cluster = std::min(ctx->max_cluster, front_cluster(a.item_count, ctx->nsm));
-  cudaError_t e = dbl ? launch_front<double>(a, ctx->max_ny, st) : launch_front<float>(a, ctx->max_ny, st);
+  cudaError_t e = dbl ? launch_front<double>(a, ctx->max_ny, ctx->max_nx, st) : launch_front<float>(a, ctx->max_ny, ctx->max_nx, st);
   CK(e, "local solve kernel");
   ctx->launches += 1;
   return check_kernel_err(ctx, st);
@@ -1028,7 +1033,7 @@ lsw_status lsw_local_solve_noalloc(lsw_ctx* ctx, int cell, const void* b, void* 
   a.max_slots = std::min(rmax, nrhs);
   a.err = ctx->d_status.as<int>() + 1;
   a.cluster = std::min(ctx->max_cluster, front_cluster(a.item_count, ctx->nsm));
-  cudaError_t e = dbl ? launch_front<double>(a, ctx->max_ny, st) : launch_front<float>(a, ctx->max_ny, st);
+  cudaError_t e = dbl ? launch_front<double>(a, ctx->max_ny, ctx->max_nx, st) : launch_front<float>(a, ctx->max_ny, ctx->max_nx, st);
   CK(e, "local solve kernel");
   ctx->launches += 2;
   return check_kernel_err(ctx, st);

@@ -45,7 +45,7 @@ bool geom_valid(const lsw_geom* g, std::string* why) {
   if (!(g->h > 0.0) || !std::isfinite(g->h)) { *why = "h must be positive"; return false; }
   int nd = 0;
   for (int J = 0; J < g->n_cells; ++J) nd = std::max(nd, dir_geom(J, g->n_cells, g->n_els_in_cell, g->pml).nd);
-  if (nd > 224) { *why = "cell side exceeds 224 DOFs (m + 6 + 2p - 1 <= 224)"; return false; }
+  if (nd > 192) { *why = "cell side exceeds 192 DOFs (m + 6 + 2p - 1 <= 192)"; return false; }
   return true;
 }
 

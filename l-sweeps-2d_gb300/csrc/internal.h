@@ -140,6 +140,8 @@ struct FrontArgs {
   int* err;               // bit 1: a bounded wait timed out
   int cluster;            // CTAs per item (thread-block cluster size)
   int stages;             // shared-memory ring depth (set by the launcher)
+  int chunk;              // factor columns per streamed chunk (set by the launcher)
+  int ksw;                // consumer column slices (set by the launcher)
 };
 // CTAs per item for a front of `items` cell solves on `nsm` SMs
 inline int front_cluster(int items, int nsm) {
@@ -148,7 +150,7 @@ inline int front_cluster(int items, int nsm) {
   return cl;
 }
 
-template <typename T> cudaError_t launch_front(const FrontArgs& a, int max_ny, cudaStream_t st);
+template <typename T> cudaError_t launch_front(const FrontArgs& a, int max_ny, int max_nx, cudaStream_t st);
 int front_rmax(bool dbl);
 int front_rpad(int n);
 template <typename T> cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* prof,

@@ -13,46 +13,56 @@
 // Work split.  An item runs on a thread-block cluster of CL CTAs; CTA c owns
 // the column range J_c of every block (contiguous in the column-major factor)
 // and the same range of every line vector.  Per line it forms the partial
-// products of all rows with its columns; the partials are exchanged through
-// distributed shared memory (each CTA sums the rows of its own range over the
-// cluster), so every SM streams 1/CL of the factor.
+// products of all rows with its columns and pushes the partial sums of each
+// row to the CTA that owns that row (st.async into the owner's shared memory,
+// completing the transaction count of the owner's per-line mbarrier; no
+// fences or remote arrives on the per-line path), so every SM streams 1/CL of
+// the factor and reads only local shared memory when it finishes a line.
 //
 // Roles inside a CTA: warp 0 is the producer that streams the CTA's column
-// chunks (CW columns, contiguous) in the order the two substitutions consume
-// them, through an NS-stage shared-memory ring (cp.async.bulk + mbarrier
-// completion); warp 1 prefetches the next line's right-hand side (forward) or
-// stored y_k (backward) into shared memory; the remaining warps are consumers
-// (16 rows each, one row pair per lane group, 4*KS column phases) that
-// accumulate in registers and reduce over phases with warp shuffles, then
-// finish each line element-wise.  Owned DOFs and trace lines are accumulated
-// with fire-and-forget global reductions.  Every wait is bounded: after ~2 s
-// of clock cycles a wait raises the CTA's abort flag and *a.err, and all later
-// waits return at once so every thread still reaches every barrier.
+// chunks (CW columns, contiguous, up to ~64 KB: one bulk copy costs ~700
+// cycles whatever its size and one issuing thread keeps one copy in flight,
+// so copies are large and two lanes issue them alternately) in the order the
+// two substitutions consume them, through an NS-stage shared-memory ring
+// (cp.async.bulk + mbarrier completion); warps 1-2 prefetch the next line's
+// right-hand side (forward) or stored y_k (backward) into shared memory;
+// warp 3 copies y_k (forward) and x_k (backward) to a per-item scratch; the
+// remaining warps are consumers: a lane owns a row pair of a 64-row group and
+// a warp one of KSW interleaved column slices, accumulating in registers with
+// no cross-lane reduction.  Line vectors and partial sums are stored
+// [column][slot] so that slot offsets are compile-time constants.  The
+// outputs (owned DOFs, trace lines, cell vectors) are written once per item
+// from the scratch by every non-producer thread after the backward pass.
+// Every wait is bounded: after ~2 s of clock cycles a wait raises the CTA's
+// abort flag and *a.err, and all later waits return at once so every thread
+// still reaches every barrier.
 //
 // The right-hand sides are never materialised: a slot builds b_k on the fly
 // from the global input (stage 1, the window of DDCheckerboard::getSeparatedRHS,
 // DDCheckerboard.cpp:3564-3674, restricted to the owned set) or from its
 // neighbours' trace lines (equivalent sources of
 // SubdomainStructured::getEquivalentSources, SubdomainStructured.cpp:1304-1465,
-// and the L-shaped traces of extractLTraces, 1468-1539).  The backward pass
-// accumulates owned DOFs into the output (reduce, DDCheckerboard.cpp:744-772)
-// and the outgoing trace lines into the trace pool.
+// and the L-shaped traces of extractLTraces, 1468-1539).  After the backward
+// pass the item's owned DOFs are accumulated into the output (reduce,
+// DDCheckerboard.cpp:744-772) and its outgoing trace lines into the trace pool.
 #include "common.cuh"
 #include "internal.h"
+
+#include <algorithm>
 
 namespace lsw {
 
 namespace {
 
-constexpr int kMaxRG = 14;            // row groups of 16 rows: ny <= 224
+constexpr int kMaxRG = 3;             // row groups of 64 rows (2 per lane): ny <= 192
+constexpr int kMaxKSW = 4;            // column slices (consumer warps per row group)
+constexpr int kAux = 4;               // producer, two helper warps, writer warp
 constexpr int kNSMax = 8;             // ring stages
 constexpr int kHdr = 256;             // barrier header bytes
 constexpr int SK_NONE = 99;           // padding slot
 constexpr long long kWaitCycles = 4000000000LL;   // ~2 s at 2 GHz
+constexpr unsigned kSuspendNs = 1000000;          // try_wait sleeps up to 1 ms (woken by the phase)
 
-template <typename T> struct FCfg;
-template <> struct FCfg<float> { static constexpr int CW = 16; };
-template <> struct FCfg<double> { static constexpr int CW = 8; };
 
 // ---------------------------------------------------------------------------
 // PTX helpers
@@ -92,19 +102,19 @@ __device__ __forceinline__ void mbar_arrive_remote(uint64_t* b, unsigned rank) {
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity) {
   unsigned ok;
   asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
-      : "r"(saddr(b)), "r"(parity)
+      : "r"(saddr(b)), "r"(parity), "r"(kSuspendNs)
       : "memory");
   return ok != 0;
 }
 __device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t* b, unsigned parity) {
   unsigned ok;
   asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2, %3;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
-      : "r"(saddr(b)), "r"(parity)
+      : "r"(saddr(b)), "r"(parity), "r"(kSuspendNs)
       : "memory");
   return ok != 0;
 }
@@ -133,18 +143,25 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
 __device__ __forceinline__ void named_sync(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
-__device__ __forceinline__ float2 ld_remote(const float2* p, unsigned rank) {
-  float2 v;
-  // "memory": must not be hoisted above the barrier wait that publishes the data
-  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(mapa(saddr(p), rank))
+// store into CTA `rank`'s shared memory; the bytes complete the transaction
+// count of that CTA's mbarrier at the same offset as `bar`
+__device__ __forceinline__ void st_async(float2* p, unsigned rank, float2 v, uint64_t* bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f32 [%0], {%1, %2}, [%3];" ::"r"(
+                   mapa(saddr(p), rank)),
+               "f"(v.x), "f"(v.y), "r"(mapa(saddr(bar), rank))
                : "memory");
-  return v;
 }
-__device__ __forceinline__ double2 ld_remote(const double2* p, unsigned rank) {
-  double2 v;
-  asm volatile("ld.shared::cluster.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "r"(mapa(saddr(p), rank))
+__device__ __forceinline__ void st_async2(float2* p, unsigned rank, float2 v0, float2 v1, uint64_t* bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(
+                   mapa(saddr(p), rank)),
+               "f"(v0.x), "f"(v0.y), "f"(v1.x), "f"(v1.y), "r"(mapa(saddr(bar), rank))
                : "memory");
-  return v;
+}
+__device__ __forceinline__ void st_async(double2* p, unsigned rank, double2 v, uint64_t* bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f64 [%0], {%1, %2}, [%3];" ::"r"(
+                   mapa(saddr(p), rank)),
+               "d"(v.x), "d"(v.y), "r"(mapa(saddr(bar), rank))
+               : "memory");
 }
 __device__ __forceinline__ void red_add(float2* p, float2 v) {
   atomicAdd(&p->x, v.x);
@@ -154,6 +171,9 @@ __device__ __forceinline__ void red_add(double2* p, double2 v) {
   atomicAdd(&p->x, v.x);
   atomicAdd(&p->y, v.y);
 }
+
+// CTA c of a cluster of CL owns rows/columns [c*ny/CL, (c+1)*ny/CL)
+__device__ __forceinline__ int owner_of(int row, int ny, int CL) { return ((row + 1) * CL - 1) / ny; }
 
 __device__ __forceinline__ bool is_line(int gnode, int m, int N) {
   // interface lines k_b(J), k_b(J)+1 for J = 0..N-2 (the trace1/traceN rows
@@ -173,15 +193,6 @@ __device__ __forceinline__ cx_t<T> rhs_elem(const FrontArgs& a, const DevCell& c
   using C = cx_t<T>;
   C z = czero<C>();
   switch (s.kind) {
-    case SK_VOLUME: {
-      const int sx = s.shift & 1, sy = (s.shift >> 1) & 1;
-      if (k < cl.ownx[sx][0] || k > cl.ownx[sx][1] || j < cl.owny[sy][0] || j > cl.owny[sy][1]) return z;
-      const int gx = cl.lox + k, gy = cl.loy + j;
-      const bool lx = is_line(gx - a.p + 1, a.m, a.N), ly = is_line(gy - a.p + 1, a.m, a.N);
-      if (lx != (bool)sx || ly != (bool)sy) return z;
-      const double2 v = a.x_in[(long long)s.rhs * a.x_stride + (long long)gx * a.n_dof + gy];
-      return to_c(v, z);
-    }
     case SK_CELLVEC: {
       const double2 v = a.x_in[(long long)s.rhs * a.x_stride + (long long)k * cl.ny + j];
       return to_c(v, z);
@@ -244,38 +255,29 @@ template <> struct Pair<double> {
   __device__ __forceinline__ void load(const double2* p) { a = p[0]; b = p[1]; }
 };
 
-template <typename C> __device__ __forceinline__ C shfl_xor_c(C v, int m) {
-  v.x = __shfl_xor_sync(0xffffffffu, v.x, m);
-  v.y = __shfl_xor_sync(0xffffffffu, v.y, m);
-  return v;
-}
-
-template <typename T, int KS, int R>
-__device__ void front_body(const FrontArgs& a, const DevItem& it, const DevCell& cl, unsigned char* smem) {
+template <typename T, int R>
+__device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it, const DevCell& cl, unsigned char* smem) {
   using C = cx_t<T>;
-  constexpr int CW = FCfg<T>::CW;
-  constexpr int NPH = 4 * KS;          // column phases per chunk
-  constexpr int CPL = CW / NPH;        // columns per lane per chunk
-  static_assert(CW % NPH == 0, "chunk width");
+  const int CW = a.chunk;              // columns per chunk, multiple of 8
+  const int KSW = a.ksw;               // column slices: consumer warps per row group
   static_assert((2 * kNSMax + 3) * 8 + 4 <= kHdr, "barrier header");
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nx = cl.nx, ny = cl.ny, ldn = cl.ldn;
-  int CL = a.cluster;
+  const int CL = a.cluster;
   const int NS = a.stages;
-  unsigned crank = CL > 1 ? cluster_rank() : 0u;
+  const unsigned crank = CL > 1 ? cluster_rank() : 0u;
   if (CL > 1 && (cluster_size() != (unsigned)CL || crank != blockIdx.x % (unsigned)CL)) {
     // the launch did not form the clusters this kernel was configured for
+    // (uniform over the CTA: every thread leaves before any barrier)
     if (threadIdx.x == 0) atomicOr(a.err, 4);
-    CL = 1;
-    crank = 0;
+    return;
   }
   const int jb = (int)crank * ny / CL, je = ((int)crank + 1) * ny / CL;
   const int nJ = je - jb;               // my columns / rows of every line
-  const int RG = (ny + 15) >> 4;
-  const int PR = 16 * RG;               // rows of a partial-sum plane
-  const int NCW = KS * RG;              // consumer warps
+  const int RG = (ny + 63) >> 6;        // row groups of 64 rows
+  const int NCW = KSW * RG;             // consumer warps
   const int NCT = NCW * 32;
-  const int NSYNC = NCT + 32;           // consumers + helper warp
+  const int NSYNC = NCT + 96;           // consumers + 2 helper warps + writer warp
   const int nch = (nJ + CW - 1) / CW;   // chunks per line
   const int nslot = it.slot_count;
   const int nline = 2 * nx - 1;         // forward 0..nx-1, backward nx-2..0
@@ -283,7 +285,7 @@ __device__ void front_body(const FrontArgs& a, const DevItem& it, const DevCell&
   // ---- shared layout ----
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);
   uint64_t* empty = full + kNSMax;
-  uint64_t* pready = empty + kNSMax;    // [2]: partial sums of a line are complete cluster-wide
+  uint64_t* pready = empty + kNSMax;    // [2]: every CTA's partial sums of my rows have landed (CL > 1)
   uint64_t* exitb = pready + 2;         // cluster-wide "done with remote shared memory"
   volatile int* abort_flag = reinterpret_cast<volatile int*>(exitb + 1);
   auto al16 = [](unsigned char* q) {
@@ -297,13 +299,27 @@ __device__ void front_body(const FrontArgs& a, const DevItem& it, const DevCell&
   // each other's partial sums by offset), so size per-rank buffers by the
   // largest column range of the cluster
   const int nJcap = (ny + CL - 1) / CL;
-  C* V = reinterpret_cast<C*>(p);       // [R][nJ]  input vector of the current line (my columns)
+  // line vectors are [column][slot], the slot index fastest
+  C* V = reinterpret_cast<C*>(p);       // [nJ][R]  input vector of the current line (my columns)
   p = al16(p + (size_t)R * nJcap * sizeof(C));
-  C* H = reinterpret_cast<C*>(p);       // [R][nJ]  helper: next right-hand side or stored y_k
+  C* H = reinterpret_cast<C*>(p);       // [nJ][R]  helper: next right-hand side or stored y_k
   p = al16(p + (size_t)R * nJcap * sizeof(C));
-  C* P = reinterpret_cast<C*>(p);       // [2][KS][R][PR] partial sums (double-buffered)
-  const size_t pbuf = (size_t)KS * R * PR;
-  p = al16(p + 2 * pbuf * sizeof(C));
+  C* XR = reinterpret_cast<C*>(p);      // [nJ][R]  raw input values of the volume slots' lead slots
+  p = al16(p + (size_t)R * nJcap * sizeof(C));
+  C* Y = reinterpret_cast<C*>(p);       // [nJ][R]  y_k staged for the writer (forward)
+  p = al16(p + (size_t)R * nJcap * sizeof(C));
+  unsigned char* colf = p;              // [nJ] bit 0: grid line; bits 1, 2: owned in y (non-shifted, shifted)
+  p = al16(p + nJcap);
+  int* lead = reinterpret_cast<int*>(p); // [R] first volume slot with the same right-hand side, -1 otherwise
+  p = al16(p + sizeof(int) * R);
+  C* wsh = reinterpret_cast<C*>(p);      // [nx] coupling of line k to k-1
+  p = al16(p + sizeof(C) * nx);
+  C* esh = reinterpret_cast<C*>(p);      // [nx] coupling of line k to k+1
+  p = al16(p + sizeof(C) * nx);
+  C* Q = reinterpret_cast<C*>(p);       // [2][CL x KSW][nJcap][R] partial sums of my rows from every CTA
+  const size_t qplane = (size_t)nJcap * R;
+  const size_t qbuf = (size_t)CL * KSW * qplane;
+  p = al16(p + 2 * qbuf * sizeof(C));
   DevSlot* sl = reinterpret_cast<DevSlot*>(p);
   p = al16(p + sizeof(DevSlot) * R);
   SlotCoef* cf = reinterpret_cast<SlotCoef*>(p);
@@ -339,11 +355,35 @@ __device__ void front_body(const FrontArgs& a, const DevItem& it, const DevCell&
     cf[tid] = c;
   }
   if (tid < it.group_count) gr[tid] = a.groups[it.group_begin + tid];
+  for (int jj = tid; jj < nJ; jj += blockDim.x) {
+    const int j = jb + jj;
+    colf[jj] = (unsigned char)((is_line(cl.loy + j - a.p + 1, a.m, a.N) ? 1 : 0) |
+                               (j >= cl.owny[0][0] && j <= cl.owny[0][1] ? 2 : 0) |
+                               (j >= cl.owny[1][0] && j <= cl.owny[1][1] ? 4 : 0));
+  }
+  for (int k = tid; k < nx; k += blockDim.x) {
+    wsh[k] = to_c(px[k], czero<C>());
+    esh[k] = to_c(px[nx + k], czero<C>());
+  }
+  if (tid < R) {
+    int l = -1;
+    if (tid < nslot) {
+      const DevSlot me = a.slots[it.slot_begin + tid];
+      if (me.kind == SK_VOLUME)
+        for (int q = 0; q <= tid; ++q) {
+          const DevSlot o = a.slots[it.slot_begin + q];
+          if (o.kind == SK_VOLUME && o.rhs == me.rhs) { l = q; break; }
+        }
+    }
+    lead[tid] = l;
+  }
   if (tid == 0) {
     *abort_flag = 0;
     for (int i = 0; i < NS; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], NCW); }
-    mbar_init(&pready[0], CL * NCW);
-    mbar_init(&pready[1], CL * NCW);
+    // one local arrive (with the expected bytes) per line; the partial sums
+    // land by st.async and complete the transaction count
+    mbar_init(&pready[0], 1);
+    mbar_init(&pready[1], 1);
     mbar_init(&exitb[0], CL * NCW);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -353,14 +393,71 @@ __device__ void front_body(const FrontArgs& a, const DevItem& it, const DevCell&
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
   }
 
+  // Outputs of the solved item, from the x_k rows in scratch (all of them are
+  // there once the backward pass is done): owned DOFs summed per (right-hand
+  // side, shift) group into the output (DDCheckerboard::reduce, 744-772), the
+  // slots' outgoing trace lines into the trace pool, and whole cell vectors
+  // for single-cell solves.  Spread over every thread but the producer's,
+  // off the per-line critical path.
+  auto epilogue = [&](int et) {
+    auto xat = [&](int k, int r, int j) { return scr[((size_t)k * ny + j) * R + r]; };
+    for (int g = 0; g < it.group_count; ++g) {
+      const DevGroup G = gr[g];
+      if (G.out_off < 0) continue;
+      const int sx = G.shift & 1, sy = (G.shift >> 1) & 1;
+      const int k0 = sx ? cl.ownx[1][0] : cl.ownx[0][0], k1 = sx ? cl.ownx[1][1] : cl.ownx[0][1];
+      const int j0 = max(sy ? cl.owny[1][0] : cl.owny[0][0], jb);
+      const int j1 = min(sy ? cl.owny[1][1] : cl.owny[0][1], je - 1);
+      const int w = j1 - j0 + 1, hg = k1 - k0 + 1;
+      if (w <= 0 || hg <= 0) continue;
+      for (int e = et; e < w * hg; e += NSYNC) {
+        const int k = k0 + e / w, j = j0 + e % w;
+        C sum = czero<C>();
+        for (int q = 0; q < G.slot_count; ++q) sum = cadd(sum, xat(k, G.slot_begin + q, j));
+        red_add(outs + G.out_off + (long long)(cl.lox + k) * a.n_dof + cl.loy + j, sum);
+      }
+    }
+    for (int r = 0; r < R; ++r) {
+      const DevSlot& sr = sl[r];
+      if (sr.kind == SK_NONE) continue;
+      if (sr.kind == SK_CELLVEC) {
+        for (int e = et; e < nx * nJ; e += NSYNC) {
+          const int k = e / nJ, j = jb + (e - (e / nJ) * nJ);
+          a.x_out[(long long)sr.rhs * a.out_stride + (long long)k * ny + j] = to_c(xat(k, r, j), make_double2(0, 0));
+        }
+        continue;
+      }
+      // trace values; where lines cross, BL2TR overwrites trace0 entries
+      // before they are added (DDCheckerboard.cpp:2520-2526)
+      auto tval = [&](int k, int j) {
+        if (sr.overwrite) {
+          if (j == sr.yo) return tr[sr.in_ud0 + k];
+          if (k == sr.xo) return tr[sr.in_lr0 + j];
+        }
+        return xat(k, r, j);
+      };
+      for (int l = 0; l < sr.n_lr; ++l) {
+        const int k = sr.lr_line[l];
+        if (k < 0 || k >= nx) continue;
+        for (int jj = et; jj < nJ; jj += NSYNC) red_add(trw + sr.lr_out[l] + jb + jj, tval(k, jb + jj));
+      }
+      for (int l = 0; l < sr.n_ud; ++l) {
+        const int j = sr.ud_line[l];
+        if (j < jb || j >= je) continue;
+        for (int k = et; k < nx; k += NSYNC) red_add(trw + sr.ud_out[l] + k, tval(k, j));
+      }
+    }
+  };
+
   // ============================ producer ============================
   if (warp == 0) {
-    if (lane == 0) {
+    if (lane < 2) {
       long long idx = 0;
       for (int li = 0; li < nline; ++li) {
         const int k = li < nx ? li : 2 * nx - 2 - li;
         const C* blk = fac + (size_t)k * ny * ldn;
         for (int c = 0; c < nch; ++c, ++idx) {
+          if ((idx & 1) != lane) continue;   // lanes 0 and 1 issue alternate chunks
           const int slot = (int)(idx % NS);
           if (idx >= NS) {
             if (!mbar_wait<false>(&empty[slot], (unsigned)(((idx / NS) - 1) & 1), a.err, abort_flag)) return;
@@ -376,76 +473,145 @@ __device__ void front_body(const FrontArgs& a, const DevItem& it, const DevCell&
     return;
   }
 
-  // ============================ helper ============================
-  if (warp == 1) {
-    // line 0 right-hand side
-    for (int e = lane; e < R * nJ; e += 32) {
-      const int r = e / nJ, j = jb + (e - r * nJ);
-      H[e] = rhs_elem<T>(a, cl, sl[r], cf[r], tr, 0, j);
-    }
+  // ============================ helpers ============================
+  if (warp == 1 || warp == 2) {
+    const int ht = tid - 32;   // 0..63
+    // right-hand side of line kk for my rows into H; the volume slots of one
+    // right-hand side share one load per DOF (each DOF lies in one window)
+    constexpr int UB = 8;      // loads in flight per helper thread
+    auto build = [&](int kk) {
+      const long long rowoff = (long long)(cl.lox + kk) * a.n_dof + cl.loy + jb;
+      for (int e0 = ht; e0 < R * nJ; e0 += 64 * UB) {
+        double2 v[UB];
+        int dst[UB];
+#pragma unroll
+        for (int u = 0; u < UB; ++u) {
+          const int e = e0 + 64 * u;
+          dst[u] = -1;
+          if (e < R * nJ) {
+            const int r = e / nJ, jj = e - r * nJ;
+            if (lead[r] == r) {
+              v[u] = a.x_in[(long long)sl[r].rhs * a.x_stride + rowoff + jj];
+              dst[u] = jj * R + r;
+            }
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < UB; ++u)
+          if (dst[u] >= 0) XR[dst[u]] = to_c(v[u], czero<C>());
+      }
+      named_sync(2, 64);
+      // the volume window of shift (sx, sy): owned DOFs whose x- and y-line
+      // status matches the shift (getSeparatedRHS)
+      const int lx = is_line(cl.lox + kk - a.p + 1, a.m, a.N) ? 1 : 0;
+      const int kx0 = (kk >= cl.ownx[0][0] && kk <= cl.ownx[0][1]) ? 1 : 0;
+      const int kx1 = (kk >= cl.ownx[1][0] && kk <= cl.ownx[1][1]) ? 1 : 0;
+      for (int e = ht; e < R * nJ; e += 64) {
+        const int jj = e / R, r = e - jj * R, j = jb + jj;
+        const DevSlot& s = sl[r];
+        C v = czero<C>();
+        if (s.kind == SK_VOLUME) {
+          const int sx = s.shift & 1, sy = (s.shift >> 1) & 1;
+          const int f = colf[jj];
+          if ((sx ? kx1 : kx0) && ((f >> (1 + sy)) & 1) && lx == sx && (f & 1) == sy) v = XR[jj * R + lead[r]];
+        } else {
+          v = rhs_elem<T>(a, cl, s, cf[r], tr, kk, j);
+        }
+        H[e] = v;
+      }
+    };
+    build(0);
     named_sync(1, NSYNC);     // S0: H = b_0
     named_sync(1, NSYNC);     // S0b: consumers copied it into V
     for (int li = 0; li < nline; ++li) {
       const bool fwd = li < nx;
       const int k = fwd ? li : 2 * nx - 2 - li;
       if (fwd) {
-        if (k + 1 < nx)
-          for (int e = lane; e < R * nJ; e += 32) {
-            const int r = e / nJ, j = jb + (e - r * nJ);
-            H[e] = rhs_elem<T>(a, cl, sl[r], cf[r], tr, k + 1, j);
-          }
+        if (k + 1 < nx) build(k + 1);
       } else {
-        const C* yk = scr + (size_t)k * R * ny;
-        for (int e = lane; e < R * nJ; e += 32) {
-          const int r = e / nJ, jj = e - r * nJ;
-          H[e] = yk[(size_t)r * ny + jb + jj];
+        const C* yk = scr + ((size_t)k * ny + jb) * R;
+        for (int e0 = ht; e0 < R * nJ; e0 += 64 * UB) {
+          C v[UB];
+#pragma unroll
+          for (int u = 0; u < UB; ++u) {
+            const int e = e0 + 64 * u;
+            if (e < R * nJ) v[u] = yk[e];
+          }
+#pragma unroll
+          for (int u = 0; u < UB; ++u)
+            if (e0 + 64 * u < R * nJ) H[e0 + 64 * u] = v[u];
         }
       }
       named_sync(1, NSYNC);   // sync1
       named_sync(1, NSYNC);   // sync2
     }
+    named_sync(1, NSYNC);     // every x_k is stored
+    epilogue(NCT + ht);
+    return;
+  }
+
+  // ============================ writer ============================
+  if (warp == 3) {
+    named_sync(1, NSYNC);     // S0
+    named_sync(1, NSYNC);     // S0b
+    for (int li = 0; li < nline; ++li) {
+      const bool fwd = li < nx;
+      const int k = fwd ? li : 2 * nx - 2 - li;
+      named_sync(1, NSYNC);   // sync1
+      named_sync(1, NSYNC);   // sync2: Y (forward y_k) or V (backward x_k) is complete
+      // forward y_k (on the last line equal to x_k), backward x_k over it
+      const C* src = fwd ? Y : V;
+      C* dst = scr + ((size_t)k * ny + jb) * R;
+      for (int e = lane; e < R * nJ; e += 32) dst[e] = src[e];
+    }
+    named_sync(1, NSYNC);     // every x_k is stored
+    epilogue(NCT + 64 + lane);
     return;
   }
 
   // ============================ consumers ============================
-  const int cw = warp - 2;
+  const int cw = warp - kAux;
   if (cw >= NCW) return;   // idle warp (small cell)
   const int ct = cw * 32 + lane;
-  const int rg = cw / KS, ks = cw % KS;
-  const int rpl = lane & 7, cs = lane >> 3;
-  const int phase = ks * 4 + cs;
-  const int r0 = rg * 16 + 2 * rpl;
+  const int rg = cw / KSW, ks = cw % KSW;
+  const int r0 = rg * 64 + 2 * lane;    // my row pair
   const bool rows_ok = r0 < ldn;
 
   named_sync(1, NSYNC);       // S0
   for (int e = ct; e < R * nJ; e += NCT) V[e] = H[e];
   named_sync(1, NSYNC);       // S0b
 
+  // bytes of partial sums that land in my Q per line: my rows x R x KSW slices x CL CTAs
+  const unsigned line_bytes = (unsigned)(nJ * R * KSW * CL * sizeof(C));
+  if (CL > 1 && ct == 0) mbar_expect_tx(&pready[0], line_bytes);
   long long idx = 0;
   for (int li = 0; li < nline; ++li) {
     const bool fwd = li < nx;
     const int k = fwd ? li : 2 * nx - 2 - li;
     const int buf = li & 1;
-    // ---- partial products of all rows with my columns ----
+    // arm the next line's barrier: its buffer was last read before the
+    // previous sync2 (peers' bytes may land before this; the phase cannot
+    // complete without this arrive)
+    if (CL > 1 && ct == 0 && li + 1 < nline) mbar_expect_tx(&pready[(li + 1) & 1], line_bytes);
+    // ---- partial products of my row pair with my slice of my columns ----
     C acc0[R], acc1[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) { acc0[r] = czero<C>(); acc1[r] = czero<C>(); }
     for (int c = 0; c < nch; ++c, ++idx) {
       const int slot = (int)(idx % NS);
       const bool ok = mbar_wait<false>(&full[slot], (unsigned)((idx / NS) & 1), a.err, abort_flag);
-      const C* S = ring + (size_t)slot * slot_elems;
+      const C* S = ring + (size_t)slot * slot_elems + r0;
       const int c0 = c * CW;
       const int ncol = min(CW, nJ - c0);
-#pragma unroll
-      for (int q = 0; q < CPL; ++q) {
-        const int cc = phase + NPH * q;
-        if (ok && cc < ncol && rows_ok) {
+      if (ok && rows_ok) {
+#pragma unroll 2
+        for (int cc = ks; cc < ncol; cc += KSW) {
           Pair<T> s;
-          s.load(S + (size_t)cc * ldn + r0);
-          const C* v = V + c0 + cc;
+          s.load(S + (size_t)cc * ldn);
+          const C* v = V + (size_t)(c0 + cc) * R;
 #pragma unroll
           for (int r = 0; r < R; ++r) {
-            const C vr = v[(size_t)r * nJ];
+            const C vr = v[r];
             cfma(acc0[r], s.a, vr);
             cfma(acc1[r], s.b, vr);
           }
@@ -454,42 +620,40 @@ __device__ void front_body(const FrontArgs& a, const DevItem& it, const DevCell&
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[slot]);
     }
+    // push the partial sums of rows r0, r0+1 to the CTA that owns them
+    C* Qb = Q + buf * qbuf;
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      acc0[r] = cadd(acc0[r], shfl_xor_c(acc0[r], 8));
-      acc0[r] = cadd(acc0[r], shfl_xor_c(acc0[r], 16));
-      acc1[r] = cadd(acc1[r], shfl_xor_c(acc1[r], 8));
-      acc1[r] = cadd(acc1[r], shfl_xor_c(acc1[r], 16));
-    }
-    C* Pb = P + buf * pbuf;
-    if (cs == 0) {
-      C* pp = Pb + (size_t)ks * R * PR + r0;
+    for (int h = 0; h < 2; ++h) {
+      const int row = r0 + h;
+      if (row < ny) {
+        const int o = owner_of(row, ny, CL);
+        C* dst = Qb + ((size_t)crank * KSW + ks) * qplane + (size_t)(row - o * ny / CL) * R;
+        if (CL == 1) {
 #pragma unroll
-      for (int r = 0; r < R; ++r) { pp[(size_t)r * PR] = acc0[r]; pp[(size_t)r * PR + 1] = acc1[r]; }
+          for (int r = 0; r < R; ++r) dst[r] = h ? acc1[r] : acc0[r];
+        } else if constexpr (sizeof(T) == 4 && R % 2 == 0) {
+#pragma unroll
+          for (int r = 0; r < R; r += 2)
+            st_async2(dst + r, (unsigned)o, h ? acc1[r] : acc0[r], h ? acc1[r + 1] : acc0[r + 1], &pready[buf]);
+        } else {
+#pragma unroll
+          for (int r = 0; r < R; ++r) st_async(dst + r, (unsigned)o, h ? acc1[r] : acc0[r], &pready[buf]);
+        }
+      }
     }
-    if (CL > 1) {
-      __syncwarp();
-      if (lane < CL) mbar_arrive_remote(&pready[buf], (unsigned)lane);
-      mbar_wait<true>(&pready[buf], (unsigned)((li >> 1) & 1), a.err, abort_flag);
-    }
+    if (CL > 1) mbar_wait<true>(&pready[buf], (unsigned)((li >> 1) & 1), a.err, abort_flag);
     named_sync(1, NSYNC);     // sync1: partials (cluster-wide) and H complete
 
     // ---- finish the line for my rows, element-wise ----
-    const C wk = (fwd && k + 1 < nx) ? to_c(px[k + 1], czero<C>()) : czero<C>();
-    const C ek = to_c(px[nx + k], czero<C>());
-    C* yk = scr + (size_t)k * R * ny;
+    const C wk = (fwd && k + 1 < nx) ? wsh[k + 1] : czero<C>();
+    const C ek = esh[k];
+    const int nplane = CL * KSW;
     for (int e = ct; e < R * nJ; e += NCT) {
-      const int r = e / nJ, jj = e - r * nJ, j = jb + jj;
       C s = czero<C>();
-      for (int cr = 0; cr < CL; ++cr) {
-#pragma unroll
-        for (int q = 0; q < KS; ++q) {
-          const C* src = Pb + ((size_t)q * R + r) * PR + j;
-          s = cadd(s, (CL > 1 && cr != (int)crank) ? ld_remote(src, (unsigned)cr) : *src);
-        }
-      }
+      const C* q = Qb + e;
+      for (int pl = 0; pl < nplane; ++pl, q += qplane) s = cadd(s, *q);
       if (fwd) {
-        yk[(size_t)r * ny + j] = s;
+        Y[e] = s;
         if (k + 1 < nx) {
           C b = H[e];
           cfms(b, wk, s);
@@ -504,43 +668,9 @@ __device__ void front_body(const FrontArgs& a, const DevItem& it, const DevCell&
       }
     }
     named_sync(1, NSYNC);     // sync2: V holds r_{k+1} (forward) or x_k
-
-    // ---- epilogue on x_k (backward, and the last forward line) ----
-    if (!fwd || k == nx - 1) {
-      const bool kx0 = k >= cl.ownx[0][0] && k <= cl.ownx[0][1];
-      const bool kx1 = k >= cl.ownx[1][0] && k <= cl.ownx[1][1];
-      const long long rowoff = (long long)(cl.lox + k) * a.n_dof + cl.loy;
-      for (int e = ct; e < it.group_count * nJ; e += NCT) {
-        const int g = e / nJ, j = jb + (e - g * nJ);
-        const DevGroup G = gr[g];
-        if (G.out_off < 0) continue;
-        const int sy = (G.shift >> 1) & 1;
-        if (!((G.shift & 1) ? kx1 : kx0) || j < cl.owny[sy][0] || j > cl.owny[sy][1]) continue;
-        C sum = czero<C>();
-        for (int q = 0; q < G.slot_count; ++q) sum = cadd(sum, V[(size_t)(G.slot_begin + q) * nJ + (j - jb)]);
-        red_add(outs + G.out_off + rowoff + j, sum);
-      }
-      for (int e = ct; e < R * nJ; e += NCT) {
-        const int r = e / nJ, jj = e - r * nJ, j = jb + jj;
-        const DevSlot& s = sl[r];
-        if (s.kind == SK_NONE) continue;
-        const C xv = V[e];
-        if (s.kind == SK_CELLVEC) {
-          a.x_out[(long long)s.rhs * a.out_stride + (long long)k * ny + j] = to_c(xv, make_double2(0, 0));
-          continue;
-        }
-        C v = xv;
-        if (s.overwrite) {
-          if (j == s.yo) v = tr[s.in_ud0 + k];
-          else if (k == s.xo) v = tr[s.in_lr0 + j];
-        }
-        for (int l = 0; l < s.n_lr; ++l)
-          if (s.lr_line[l] == k) red_add(trw + s.lr_out[l] + j, v);
-        for (int l = 0; l < s.n_ud; ++l)
-          if (s.ud_line[l] == j) red_add(trw + s.ud_out[l] + k, v);
-      }
-    }
   }
+  named_sync(1, NSYNC);       // every x_k is stored
+  epilogue(ct);
 
   if (CL > 1) {
     // nobody leaves while a peer may still read its partial sums
@@ -550,45 +680,35 @@ __device__ void front_body(const FrontArgs& a, const DevItem& it, const DevCell&
   }
 }
 
-// register budget: the warps of a CTA spread over the 4 sub-partitions of an
-// SM, each with 16K registers: 16 warps (KS = 1) -> 128, 30 warps -> 64
-template <int KS> struct RegCap;
-template <> struct RegCap<1> { static constexpr int v = 128; };   // 512 threads
-template <> struct RegCap<2> { static constexpr int v = 64; };    // 960 threads
-
-template <typename T, int KS>
-__global__ void __maxnreg__(RegCap<KS>::v) k_front(FrontArgs a) {
+// 16 warps (4 auxiliary + up to 3 row groups x 4 column slices) x 128 registers
+template <typename T>
+__global__ void __maxnreg__(128) k_front(FrontArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const DevItem it = a.items[blockIdx.x / a.cluster];
   const DevCell cl = a.cells[it.cell];
   const int n = it.slot_count;
-  if constexpr (sizeof(T) == 4 && KS == 1) {
-    if (n <= 1) front_body<T, KS, 1>(a, it, cl, smem);
-    else if (n <= 2) front_body<T, KS, 2>(a, it, cl, smem);
-    else if (n <= 4) front_body<T, KS, 4>(a, it, cl, smem);
-    else if (n <= 8) front_body<T, KS, 8>(a, it, cl, smem);
-    else if (n <= 12) front_body<T, KS, 12>(a, it, cl, smem);
-    else front_body<T, KS, 16>(a, it, cl, smem);
-  } else if constexpr (KS == 2) {
-    if (n <= 1) front_body<T, KS, 1>(a, it, cl, smem);
-    else if (n <= 2) front_body<T, KS, 2>(a, it, cl, smem);
-    else front_body<T, KS, 4>(a, it, cl, smem);
+  if constexpr (sizeof(T) == 4) {
+    if (n <= 1) front_body<T, 1>(a, it, cl, smem);
+    else if (n <= 2) front_body<T, 2>(a, it, cl, smem);
+    else if (n <= 4) front_body<T, 4>(a, it, cl, smem);
+    else if (n <= 8) front_body<T, 8>(a, it, cl, smem);
+    else if (n <= 12) front_body<T, 12>(a, it, cl, smem);
+    else front_body<T, 16>(a, it, cl, smem);
   } else {
-    if (n <= 1) front_body<T, KS, 1>(a, it, cl, smem);
-    else if (n <= 2) front_body<T, KS, 2>(a, it, cl, smem);
-    else if (n <= 4) front_body<T, KS, 4>(a, it, cl, smem);
-    else front_body<T, KS, 8>(a, it, cl, smem);
+    if (n <= 1) front_body<T, 1>(a, it, cl, smem);
+    else if (n <= 2) front_body<T, 2>(a, it, cl, smem);
+    else if (n <= 4) front_body<T, 4>(a, it, cl, smem);
+    else front_body<T, 8>(a, it, cl, smem);
   }
 }
 
 template <typename T>
-size_t smem_need(int ldn_max, int ny_max, int R, int KS, int CL, int NS) {
+size_t smem_need(int ldn_max, int ny_max, int nx_max, int R, int KSW, int CL, int CW, int NS) {
   using C = cx_t<T>;
-  const int RG = (ny_max + 15) / 16;
   const int nJ = (ny_max + CL - 1) / CL + 1;
-  return kHdr + (size_t)NS * FCfg<T>::CW * ldn_max * sizeof(C) + 2 * (size_t)R * nJ * sizeof(C) +
-         2 * (size_t)KS * R * 16 * RG * sizeof(C) +
-         (size_t)R * (sizeof(DevSlot) + sizeof(SlotCoef) + sizeof(DevGroup)) + 6 * 16;
+  return kHdr + (size_t)NS * CW * ldn_max * sizeof(C) + 4 * (size_t)R * nJ * sizeof(C) + 4 * R + nJ + 16 +
+         2 * (size_t)CL * KSW * R * nJ * sizeof(C) + 2 * (size_t)nx_max * sizeof(C) +
+         (size_t)R * (sizeof(DevSlot) + sizeof(SlotCoef) + sizeof(DevGroup)) + 11 * 16;
 }
 
 }  // namespace
@@ -597,23 +717,35 @@ int front_rmax(bool dbl) { return dbl ? 8 : 16; }
 int front_rpad(int n) { return n <= 1 ? 1 : n <= 2 ? 2 : n <= 4 ? 4 : n <= 8 ? 8 : n <= 12 ? 12 : 16; }
 
 template <typename T>
-cudaError_t launch_front(const FrontArgs& a_in, int max_ny, cudaStream_t st) {
+cudaError_t launch_front(const FrontArgs& a_in, int max_ny, int max_nx, cudaStream_t st) {
   if (a_in.item_count <= 0) return cudaSuccess;
   FrontArgs a = a_in;
   const bool dbl = sizeof(T) == 8;
   const int ldn = (max_ny + 3) & ~3;
-  // two consumer warps per row group for small slot counts (float)
-  const int KS = (!dbl && a.max_slots <= 4) ? 2 : 1;
-  const int R = dbl ? 8 : (KS == 2 ? 4 : 16);
+  const int R = std::min(front_rpad(std::max(1, a.max_slots)), front_rmax(dbl));
   if (a.cluster < 1) a.cluster = 1;
   int dev = 0, maxopt = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  int NS = kNSMax;
-  while (NS > 2 && smem_need<T>(ldn, max_ny, R, KS, a.cluster, NS) > (size_t)maxopt) --NS;
+  // largest chunk (columns, multiple of 8, <= ~64 KB) and then the deepest ring that fit
+  const int nJmax = (max_ny + a.cluster - 1) / a.cluster;
+  // column slices: as many as keep >= 8 columns per slice and the partial-sum
+  // buffers (2 x KSW x R x ny) within 48 KB
+  int KSW = kMaxKSW;
+  while (KSW > 1 && (nJmax < 4 * KSW || 2 * (size_t)KSW * R * max_ny * sizeof(cx_t<T>) > 49152)) --KSW;
+  a.ksw = KSW;
+  const int cwmax = (int)std::min<size_t>(((size_t)65536 / ((size_t)ldn * sizeof(cx_t<T>))) & ~size_t(7),
+                                          (size_t)((nJmax + 7) & ~7));
+  int CW = std::max(8, cwmax), NS = 0;
+  for (; CW >= 8; CW -= 8) {
+    for (NS = 4; NS >= 2; --NS)
+      if (smem_need<T>(ldn, max_ny, max_nx, R, KSW, a.cluster, CW, NS) <= (size_t)maxopt) break;
+    if (NS >= 2) break;
+  }
+  if (CW < 8) return cudaErrorInvalidConfiguration;
   a.stages = NS;
-  const size_t smem = smem_need<T>(ldn, max_ny, R, KS, a.cluster, NS);
-  if (smem > (size_t)maxopt) return cudaErrorInvalidConfiguration;
+  a.chunk = CW;
+  const size_t smem = smem_need<T>(ldn, max_ny, max_nx, R, KSW, a.cluster, CW, NS);
   cudaLaunchConfig_t cfg{};
   cudaLaunchAttribute attr[1];
   cfg.gridDim = dim3((unsigned)(a.item_count * a.cluster));
@@ -625,24 +757,14 @@ cudaError_t launch_front(const FrontArgs& a_in, int max_ny, cudaStream_t st) {
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaError_t e;
-  if constexpr (sizeof(T) == 4) {
-    if (KS == 2) {
-      auto kern = k_front<T, 2>;
-      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-      cfg.blockDim = dim3(64 + 2 * kMaxRG * 32);
-      return cudaLaunchKernelEx(&cfg, kern, a);
-    }
-  }
-  auto kern = k_front<T, 1>;
-  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  auto kern = k_front<T>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  cfg.blockDim = dim3(64 + kMaxRG * 32);
+  cfg.blockDim = dim3(32 * (kAux + kMaxRG * kMaxKSW));
   return cudaLaunchKernelEx(&cfg, kern, a);
 }
 
-template cudaError_t launch_front<float>(const FrontArgs&, int, cudaStream_t);
-template cudaError_t launch_front<double>(const FrontArgs&, int, cudaStream_t);
+template cudaError_t launch_front<float>(const FrontArgs&, int, int, cudaStream_t);
+template cudaError_t launch_front<double>(const FrontArgs&, int, int, cudaStream_t);
 
 }  // namespace lsw
