@@ -304,22 +304,24 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   p = al16(p + (size_t)R * nJcap * sizeof(C));
   C* H = reinterpret_cast<C*>(p);       // [nJ][R]  helper: next right-hand side or stored y_k
   p = al16(p + (size_t)R * nJcap * sizeof(C));
-  C* XR = reinterpret_cast<C*>(p);      // [nJ][R]  raw input values of the volume slots' lead slots
-  p = al16(p + (size_t)R * nJcap * sizeof(C));
   C* Y = reinterpret_cast<C*>(p);       // [nJ][R]  y_k staged for the writer (forward)
   p = al16(p + (size_t)R * nJcap * sizeof(C));
   unsigned char* colf = p;              // [nJ] bit 0: grid line; bits 1, 2: owned in y (non-shifted, shifted)
   p = al16(p + nJcap);
-  int* lead = reinterpret_cast<int*>(p); // [R] first volume slot with the same right-hand side, -1 otherwise
-  p = al16(p + sizeof(int) * R);
+  unsigned char* linef = p;             // [nx] bit 0: grid line; bits 1, 2: owned in x (non-shifted, shifted)
+  p = al16(p + nx);
   C* wsh = reinterpret_cast<C*>(p);      // [nx] coupling of line k to k-1
   p = al16(p + sizeof(C) * nx);
   C* esh = reinterpret_cast<C*>(p);      // [nx] coupling of line k to k+1
   p = al16(p + sizeof(C) * nx);
-  C* Q = reinterpret_cast<C*>(p);       // [2][CL x KSW][nJcap][R] partial sums of my rows from every CTA
+  C* Q = reinterpret_cast<C*>(p);       // [2][CL][nJcap][R] partial sums of my rows from every CTA
   const size_t qplane = (size_t)nJcap * R;
-  const size_t qbuf = (size_t)CL * KSW * qplane;
+  const size_t qbuf = (size_t)CL * qplane;
   p = al16(p + 2 * qbuf * sizeof(C));
+  C* LS = reinterpret_cast<C*>(p);      // [KSW][64 RG][R] the column slices' partial sums, before their sum
+  p = al16(p + (size_t)KSW * 64 * RG * R * sizeof(C));
+  int* rowinfo = reinterpret_cast<int*>(p);   // [ny] owner CTA << 16 | row offset in the owner's range
+  p = al16(p + sizeof(int) * ny);
   DevSlot* sl = reinterpret_cast<DevSlot*>(p);
   p = al16(p + sizeof(DevSlot) * R);
   SlotCoef* cf = reinterpret_cast<SlotCoef*>(p);
@@ -355,6 +357,14 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
     cf[tid] = c;
   }
   if (tid < it.group_count) gr[tid] = a.groups[it.group_begin + tid];
+  for (int row = tid; row < ny; row += blockDim.x) {
+    const int o = owner_of(row, ny, CL);
+    rowinfo[row] = (o << 16) | (row - o * ny / CL);
+  }
+  for (int k = tid; k < nx; k += blockDim.x)
+    linef[k] = (unsigned char)((is_line(cl.lox + k - a.p + 1, a.m, a.N) ? 1 : 0) |
+                               (k >= cl.ownx[0][0] && k <= cl.ownx[0][1] ? 2 : 0) |
+                               (k >= cl.ownx[1][0] && k <= cl.ownx[1][1] ? 4 : 0));
   for (int jj = tid; jj < nJ; jj += blockDim.x) {
     const int j = jb + jj;
     colf[jj] = (unsigned char)((is_line(cl.loy + j - a.p + 1, a.m, a.N) ? 1 : 0) |
@@ -364,18 +374,6 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   for (int k = tid; k < nx; k += blockDim.x) {
     wsh[k] = to_c(px[k], czero<C>());
     esh[k] = to_c(px[nx + k], czero<C>());
-  }
-  if (tid < R) {
-    int l = -1;
-    if (tid < nslot) {
-      const DevSlot me = a.slots[it.slot_begin + tid];
-      if (me.kind == SK_VOLUME)
-        for (int q = 0; q <= tid; ++q) {
-          const DevSlot o = a.slots[it.slot_begin + q];
-          if (o.kind == SK_VOLUME && o.rhs == me.rhs) { l = q; break; }
-        }
-    }
-    lead[tid] = l;
   }
   if (tid == 0) {
     *abort_flag = 0;
@@ -392,6 +390,31 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
     // every CTA's barriers are initialised before anyone arrives remotely
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
   }
+
+  // Right-hand sides of every line of the item into its scratch rows (row k
+  // then holds b_k until the forward pass replaces it with y_k, and the
+  // backward pass with x_k), computed once per item by every non-producer
+  // thread so that the per-line helpers only copy a contiguous row.
+  // A volume slot of shift (sx, sy) takes the owned DOFs whose x- and y-line
+  // status matches the shift (the windows of getSeparatedRHS).
+  auto prologue = [&](int et) {
+    const int per_line = nJ * R;
+    for (int e = et; e < nx * per_line; e += NSYNC) {
+      const int k = e / per_line, rem = e - k * per_line;
+      const int jj = rem / R, r = rem - jj * R, j = jb + jj;
+      const DevSlot& sr = sl[r];
+      C v = czero<C>();
+      if (sr.kind == SK_VOLUME) {
+        const int sx = sr.shift & 1, sy = (sr.shift >> 1) & 1;
+        const int fx = linef[k], fy = colf[jj];
+        if (((fx >> (1 + sx)) & 1) && ((fy >> (1 + sy)) & 1) && (fx & 1) == sx && (fy & 1) == sy)
+          v = to_c(a.x_in[(long long)sr.rhs * a.x_stride + (long long)(cl.lox + k) * a.n_dof + cl.loy + j], czero<C>());
+      } else if (sr.kind != SK_NONE) {
+        v = rhs_elem<T>(a, cl, sr, cf[r], tr, k, j);
+      }
+      scr[((size_t)k * ny + jb) * R + rem] = v;
+    }
+  };
 
   // Outputs of the solved item, from the x_k rows in scratch (all of them are
   // there once the backward pass is done): owned DOFs summed per (right-hand
@@ -476,71 +499,32 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   // ============================ helpers ============================
   if (warp == 1 || warp == 2) {
     const int ht = tid - 32;   // 0..63
-    // right-hand side of line kk for my rows into H; the volume slots of one
-    // right-hand side share one load per DOF (each DOF lies in one window)
     constexpr int UB = 8;      // loads in flight per helper thread
-    auto build = [&](int kk) {
-      const long long rowoff = (long long)(cl.lox + kk) * a.n_dof + cl.loy + jb;
+    // scratch row `row` (b_row, y_row) of my columns into H
+    auto fetch = [&](int row) {
+      const C* src = scr + ((size_t)row * ny + jb) * R;
       for (int e0 = ht; e0 < R * nJ; e0 += 64 * UB) {
-        double2 v[UB];
-        int dst[UB];
-#pragma unroll
-        for (int u = 0; u < UB; ++u) {
-          const int e = e0 + 64 * u;
-          dst[u] = -1;
-          if (e < R * nJ) {
-            const int r = e / nJ, jj = e - r * nJ;
-            if (lead[r] == r) {
-              v[u] = a.x_in[(long long)sl[r].rhs * a.x_stride + rowoff + jj];
-              dst[u] = jj * R + r;
-            }
-          }
-        }
+        C v[UB];
 #pragma unroll
         for (int u = 0; u < UB; ++u)
-          if (dst[u] >= 0) XR[dst[u]] = to_c(v[u], czero<C>());
-      }
-      named_sync(2, 64);
-      // the volume window of shift (sx, sy): owned DOFs whose x- and y-line
-      // status matches the shift (getSeparatedRHS)
-      const int lx = is_line(cl.lox + kk - a.p + 1, a.m, a.N) ? 1 : 0;
-      const int kx0 = (kk >= cl.ownx[0][0] && kk <= cl.ownx[0][1]) ? 1 : 0;
-      const int kx1 = (kk >= cl.ownx[1][0] && kk <= cl.ownx[1][1]) ? 1 : 0;
-      for (int e = ht; e < R * nJ; e += 64) {
-        const int jj = e / R, r = e - jj * R, j = jb + jj;
-        const DevSlot& s = sl[r];
-        C v = czero<C>();
-        if (s.kind == SK_VOLUME) {
-          const int sx = s.shift & 1, sy = (s.shift >> 1) & 1;
-          const int f = colf[jj];
-          if ((sx ? kx1 : kx0) && ((f >> (1 + sy)) & 1) && lx == sx && (f & 1) == sy) v = XR[jj * R + lead[r]];
-        } else {
-          v = rhs_elem<T>(a, cl, s, cf[r], tr, kk, j);
-        }
-        H[e] = v;
+          if (e0 + 64 * u < R * nJ) v[u] = src[e0 + 64 * u];
+#pragma unroll
+        for (int u = 0; u < UB; ++u)
+          if (e0 + 64 * u < R * nJ) H[e0 + 64 * u] = v[u];
       }
     };
-    build(0);
+    prologue(NCT + ht);
+    named_sync(1, NSYNC);     // every b_k is in scratch
+    fetch(0);
     named_sync(1, NSYNC);     // S0: H = b_0
     named_sync(1, NSYNC);     // S0b: consumers copied it into V
     for (int li = 0; li < nline; ++li) {
       const bool fwd = li < nx;
       const int k = fwd ? li : 2 * nx - 2 - li;
       if (fwd) {
-        if (k + 1 < nx) build(k + 1);
+        if (k + 1 < nx) fetch(k + 1);   // b_{k+1}
       } else {
-        const C* yk = scr + ((size_t)k * ny + jb) * R;
-        for (int e0 = ht; e0 < R * nJ; e0 += 64 * UB) {
-          C v[UB];
-#pragma unroll
-          for (int u = 0; u < UB; ++u) {
-            const int e = e0 + 64 * u;
-            if (e < R * nJ) v[u] = yk[e];
-          }
-#pragma unroll
-          for (int u = 0; u < UB; ++u)
-            if (e0 + 64 * u < R * nJ) H[e0 + 64 * u] = v[u];
-        }
+        fetch(k);                       // y_k
       }
       named_sync(1, NSYNC);   // sync1
       named_sync(1, NSYNC);   // sync2
@@ -552,6 +536,8 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
 
   // ============================ writer ============================
   if (warp == 3) {
+    prologue(NCT + 64 + lane);
+    named_sync(1, NSYNC);     // every b_k is in scratch
     named_sync(1, NSYNC);     // S0
     named_sync(1, NSYNC);     // S0b
     for (int li = 0; li < nline; ++li) {
@@ -577,12 +563,14 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   const int r0 = rg * 64 + 2 * lane;    // my row pair
   const bool rows_ok = r0 < ldn;
 
+  prologue(ct);
+  named_sync(1, NSYNC);       // every b_k is in scratch
   named_sync(1, NSYNC);       // S0
   for (int e = ct; e < R * nJ; e += NCT) V[e] = H[e];
   named_sync(1, NSYNC);       // S0b
 
-  // bytes of partial sums that land in my Q per line: my rows x R x KSW slices x CL CTAs
-  const unsigned line_bytes = (unsigned)(nJ * R * KSW * CL * sizeof(C));
+  // bytes of partial sums that land in my Q per line: my rows x R x CL CTAs
+  const unsigned line_bytes = (unsigned)(nJ * R * CL * sizeof(C));
   if (CL > 1 && ct == 0) mbar_expect_tx(&pready[0], line_bytes);
   long long idx = 0;
   for (int li = 0; li < nline; ++li) {
@@ -620,24 +608,38 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[slot]);
     }
-    // push the partial sums of rows r0, r0+1 to the CTA that owns them
+    // sum the row group's column slices in shared memory, then push each
+    // row's sum to the CTA that owns the row
+    {
+      C* ls = LS + ((size_t)ks * 64 * RG + r0) * R;
+#pragma unroll
+      for (int r = 0; r < R; ++r) { ls[r] = acc0[r]; ls[R + r] = acc1[r]; }
+    }
+    named_sync(3 + rg, KSW * 32);
     C* Qb = Q + buf * qbuf;
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int row = r0 + h;
-      if (row < ny) {
-        const int o = owner_of(row, ny, CL);
-        C* dst = Qb + ((size_t)crank * KSW + ks) * qplane + (size_t)(row - o * ny / CL) * R;
+    {
+      constexpr int UP = (sizeof(T) == 4 && R % 2 == 0) ? 2 : 1;   // complex values per store
+      constexpr int NU = R / UP;                                  // stores per row
+      const size_t lsplane = (size_t)64 * RG * R;
+      for (int u = ks * 32 + lane; u < 64 * NU; u += KSW * 32) {
+        const int rr = u / NU, up = u - rr * NU;
+        const int row = rg * 64 + rr;
+        if (row >= ny) break;
+        const C* src = LS + (size_t)row * R + up * UP;
+        C v0 = src[0], v1 = UP == 2 ? src[1] : czero<C>();
+        for (int q = 1; q < KSW; ++q) {
+          v0 = cadd(v0, src[q * lsplane]);
+          if (UP == 2) v1 = cadd(v1, src[q * lsplane + 1]);
+        }
+        const int info = rowinfo[row];
+        C* dst = Qb + ((size_t)crank * nJcap + (info & 0xffff)) * R + up * UP;
         if (CL == 1) {
-#pragma unroll
-          for (int r = 0; r < R; ++r) dst[r] = h ? acc1[r] : acc0[r];
-        } else if constexpr (sizeof(T) == 4 && R % 2 == 0) {
-#pragma unroll
-          for (int r = 0; r < R; r += 2)
-            st_async2(dst + r, (unsigned)o, h ? acc1[r] : acc0[r], h ? acc1[r + 1] : acc0[r + 1], &pready[buf]);
+          dst[0] = v0;
+          if (UP == 2) dst[1] = v1;
+        } else if constexpr (UP == 2) {
+          st_async2(dst, (unsigned)(info >> 16), v0, v1, &pready[buf]);
         } else {
-#pragma unroll
-          for (int r = 0; r < R; ++r) st_async(dst + r, (unsigned)o, h ? acc1[r] : acc0[r], &pready[buf]);
+          st_async(dst, (unsigned)(info >> 16), v0, &pready[buf]);
         }
       }
     }
@@ -647,7 +649,7 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
     // ---- finish the line for my rows, element-wise ----
     const C wk = (fwd && k + 1 < nx) ? wsh[k + 1] : czero<C>();
     const C ek = esh[k];
-    const int nplane = CL * KSW;
+    const int nplane = CL;
     for (int e = ct; e < R * nJ; e += NCT) {
       C s = czero<C>();
       const C* q = Qb + e;
@@ -706,8 +708,9 @@ template <typename T>
 size_t smem_need(int ldn_max, int ny_max, int nx_max, int R, int KSW, int CL, int CW, int NS) {
   using C = cx_t<T>;
   const int nJ = (ny_max + CL - 1) / CL + 1;
-  return kHdr + (size_t)NS * CW * ldn_max * sizeof(C) + 4 * (size_t)R * nJ * sizeof(C) + 4 * R + nJ + 16 +
-         2 * (size_t)CL * KSW * R * nJ * sizeof(C) + 2 * (size_t)nx_max * sizeof(C) +
+  return kHdr + (size_t)NS * CW * ldn_max * sizeof(C) + 3 * (size_t)R * nJ * sizeof(C) + nx_max + nJ + 32 +
+         2 * (size_t)CL * R * nJ * sizeof(C) + (size_t)KSW * 64 * kMaxRG * R * sizeof(C) + 4 * (size_t)ny_max +
+         2 * (size_t)nx_max * sizeof(C) +
          (size_t)R * (sizeof(DevSlot) + sizeof(SlotCoef) + sizeof(DevGroup)) + 11 * 16;
 }
 
@@ -729,10 +732,10 @@ cudaError_t launch_front(const FrontArgs& a_in, int max_ny, int max_nx, cudaStre
   cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   // largest chunk (columns, multiple of 8, <= ~64 KB) and then the deepest ring that fit
   const int nJmax = (max_ny + a.cluster - 1) / a.cluster;
-  // column slices: as many as keep >= 8 columns per slice and the partial-sum
-  // buffers (2 x KSW x R x ny) within 48 KB
+  // column slices: as many as keep >= 4 columns per slice and the slices'
+  // partial-sum staging (KSW x 192 x R) within 64 KB
   int KSW = kMaxKSW;
-  while (KSW > 1 && (nJmax < 4 * KSW || 2 * (size_t)KSW * R * max_ny * sizeof(cx_t<T>) > 49152)) --KSW;
+  while (KSW > 1 && (nJmax < 4 * KSW || (size_t)KSW * 64 * kMaxRG * R * sizeof(cx_t<T>) > 65536)) --KSW;
   a.ksw = KSW;
   const int cwmax = (int)std::min<size_t>(((size_t)65536 / ((size_t)ldn * sizeof(cx_t<T>))) & ~size_t(7),
                                           (size_t)((nJmax + 7) & ~7));
