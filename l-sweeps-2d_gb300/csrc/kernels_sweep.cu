@@ -318,7 +318,7 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   const size_t qplane = (size_t)nJcap * R;
   const size_t qbuf = (size_t)CL * qplane;
   p = al16(p + 2 * qbuf * sizeof(C));
-  C* LS = reinterpret_cast<C*>(p);      // [KSW][64 RG][R] the column slices' partial sums, before their sum
+  C* LS = reinterpret_cast<C*>(p);      // [KSW][R][64 RG] the column slices' partial sums, before their sum
   p = al16(p + (size_t)KSW * 64 * RG * R * sizeof(C));
   int* rowinfo = reinterpret_cast<int*>(p);   // [ny] owner CTA << 16 | row offset in the owner's range
   p = al16(p + sizeof(int) * ny);
@@ -610,26 +610,29 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
     }
     // sum the row group's column slices in shared memory, then push each
     // row's sum to the CTA that owns the row
+    // (rows fastest: a lane's row pair is one 16-byte store per slot for
+    // float, and consecutive lanes hit consecutive banks)
+    const int RG64 = 64 * RG;
     {
-      C* ls = LS + ((size_t)ks * 64 * RG + r0) * R;
+      C* ls = LS + (size_t)ks * R * RG64 + r0;
 #pragma unroll
-      for (int r = 0; r < R; ++r) { ls[r] = acc0[r]; ls[R + r] = acc1[r]; }
+      for (int r = 0; r < R; ++r) { ls[(size_t)r * RG64] = acc0[r]; ls[(size_t)r * RG64 + 1] = acc1[r]; }
     }
     named_sync(3 + rg, KSW * 32);
     C* Qb = Q + buf * qbuf;
     {
-      constexpr int UP = (sizeof(T) == 4 && R % 2 == 0) ? 2 : 1;   // complex values per store
+      constexpr int UP = (sizeof(T) == 4 && R % 2 == 0) ? 2 : 1;   // slots per store
       constexpr int NU = R / UP;                                  // stores per row
-      const size_t lsplane = (size_t)64 * RG * R;
+      const size_t lsplane = (size_t)R * RG64;
       for (int u = ks * 32 + lane; u < 64 * NU; u += KSW * 32) {
-        const int rr = u / NU, up = u - rr * NU;
+        const int up = u >> 6, rr = u & 63;   // consecutive lanes take consecutive rows
         const int row = rg * 64 + rr;
-        if (row >= ny) break;
-        const C* src = LS + (size_t)row * R + up * UP;
-        C v0 = src[0], v1 = UP == 2 ? src[1] : czero<C>();
+        if (row >= ny) continue;
+        const C* src = LS + (size_t)up * UP * RG64 + row;
+        C v0 = src[0], v1 = UP == 2 ? src[RG64] : czero<C>();
         for (int q = 1; q < KSW; ++q) {
           v0 = cadd(v0, src[q * lsplane]);
-          if (UP == 2) v1 = cadd(v1, src[q * lsplane + 1]);
+          if (UP == 2) v1 = cadd(v1, src[q * lsplane + RG64]);
         }
         const int info = rowinfo[row];
         C* dst = Qb + ((size_t)crank * nJcap + (info & 0xffff)) * R + up * UP;
