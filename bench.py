@@ -321,6 +321,7 @@ def run_gpu(args):
                          "frac": achieved / peak if peak else None, "traffic": traffic,
                          "kernel": "k_front (sweep-front cell solves), all fronts of one apply",
                          "peak_kind": peak_kind, "alg_bytes_per_apply": pr["alg_bytes"],
+                         "streamed_bytes_per_apply": pr["streamed_bytes"],
                          "front_ms_per_apply": front_ms, "fronts": pr["fronts"], "items": pr["items"],
                          "slots": pr["slots"], "apply_ms": pr["total_ms"]},
             "cpu_baseline": cpu,

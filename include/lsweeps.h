@@ -95,13 +95,15 @@ typedef struct lsw_problem_info {
  * front launch on the caller's stream). */
 typedef struct lsw_apply_profile {
   int fronts;            /* front launches per apply */
-  int items;             /* cell solves (CTAs) per apply */
+  int items;             /* front items (a cell and up to 16 of its right-hand sides) per apply */
   int slots;             /* right-hand sides over all cell solves */
   double front_ms;       /* summed device time of the front kernels */
   double total_ms;       /* device time of the whole apply */
-  double alg_bytes;      /* algorithmic bytes of the front kernels: per cell solve
-                            2 F + 4 R nx ny s, F = nx ny^2 s the factor, R slots */
-  double alg_flops;      /* 2 x 8 nx ny^2 R real flops per cell solve */
+  double alg_bytes;      /* algorithmic bytes of the front kernels: per cell and front
+                            2 F + 4 R nx ny s, F = nx ny^2 s the factor, R its slots */
+  double alg_flops;      /* 2 x 8 nx ny^2 R real flops per cell and front */
+  double streamed_bytes; /* bytes the items stream: a cell whose slots are split over
+                            several items reads its (padded) factor once per item */
 } lsw_apply_profile;
 
 /* One subdomain (SubdomainStructured) in local DOF coordinates:

@@ -146,7 +146,14 @@ lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out) {
     std::unique_ptr<Schedule> sc(new Schedule);
     std::vector<DevItem> items; std::vector<DevSlot> slots; std::vector<DevGroup> groups;
     try {
-      build_schedule(ctx->cells, ctx->N, nrhs, front_rmax(dbl), ctx->LP, sc->fronts, items, slots, groups, ctx->n2);
+      FrontPlan plan;
+      plan.cluster_cap = ctx->max_cluster;
+      plan.rmax = front_rmax(dbl);
+      plan.csize = dbl ? 16 : 8;
+      plan.col_cost = dbl ? 30.0 : 15.0;
+      for (int cl = 1; cl <= 8; cl *= 2) plan.max_clusters[cl] = front_max_clusters(dbl, cl);
+      if (plan.max_clusters[1] <= 0) plan.max_clusters[1] = ctx->nsm;
+      build_schedule(ctx->cells, ctx->N, nrhs, plan, ctx->LP, sc->fronts, items, slots, groups, ctx->n2);
     } catch (const std::exception& ex) {
       return fail(ctx, LSW_ERR_UNSUPPORTED, ex.what());
     }
@@ -199,7 +206,7 @@ lsw_status precond_impl(lsw_ctx* ctx, const double2* x, double2* y, int nrhs, cu
     a.items = sc->d_items + f.item_begin;
     a.item_count = f.item_count;
     a.max_slots = f.max_slots;
-    a.cluster = std::min(ctx->max_cluster, front_cluster(f.item_count, ctx->nsm));
+    a.cluster = f.cluster;
     if (ctx->front_events) CK(cudaEventRecord((*ctx->front_events)[2 * fi], st), "event");
     cudaError_t e = ctx->prec == LSW_PREC_C64 ? launch_front<float>(a, ctx->max_ny, ctx->max_nx, st)
                                               : launch_front<double>(a, ctx->max_ny, ctx->max_nx, st);
@@ -509,7 +516,7 @@ lsw_status lsw_apply_precond_profiled(lsw_ctx* ctx, const void* x, void* y, int 
     if (log_fronts) {
       const Front& fr = sc->fronts[f];
       std::fprintf(stderr, "front %zu items %d max_slots %d cluster %d ms %.4f\n", f, fr.item_count, fr.max_slots,
-                   std::min(ctx->max_cluster, front_cluster(fr.item_count, ctx->nsm)), ms);
+                   fr.cluster, ms);
     }
   }
   float tot = 0.f;
@@ -518,15 +525,26 @@ lsw_status lsw_apply_precond_profiled(lsw_ctx* ctx, const void* x, void* y, int 
   // algorithmic bytes / flops from the schedule
   std::vector<DevItem> items(sc->fronts.empty() ? 0 : sc->fronts.back().item_begin + sc->fronts.back().item_count);
   CK(cudaMemcpy(items.data(), sc->d_items, items.size() * sizeof(DevItem), cudaMemcpyDeviceToHost), "D2H items");
+  // algorithmic bytes count each cell's factor once per front (forward and
+  // backward pass) however its slots are split into items; the streamed
+  // bytes count every item's pass
   const double cs = (double)csize(ctx->prec);
-  double bytes = 0.0, flops = 0.0;
+  double bytes = 0.0, flops = 0.0, streamed = 0.0;
   int slots = 0;
-  for (const DevItem& it : items) {
-    const DevCell& c = ctx->cells[it.cell];
-    const double F = (double)c.nx * c.ny * c.ny * cs;
-    bytes += 2.0 * F + 4.0 * it.slot_count * (double)c.nx * c.ny * cs;
-    flops += 2.0 * 8.0 * (double)c.nx * c.ny * c.ny * it.slot_count;
-    slots += it.slot_count;
+  for (const Front& fr : sc->fronts) {
+    std::map<int, int> per_cell;
+    for (int i = fr.item_begin; i < fr.item_begin + fr.item_count; ++i) per_cell[items[i].cell] += items[i].slot_count;
+    for (const auto& kv : per_cell) {
+      const DevCell& c = ctx->cells[kv.first];
+      const double F = (double)c.nx * c.ny * c.ny * cs;
+      bytes += 2.0 * F + 4.0 * kv.second * (double)c.nx * c.ny * cs;
+      flops += 2.0 * 8.0 * (double)c.nx * c.ny * c.ny * kv.second;
+      slots += kv.second;
+    }
+    for (int i = fr.item_begin; i < fr.item_begin + fr.item_count; ++i) {
+      const DevCell& c = ctx->cells[items[i].cell];
+      streamed += 2.0 * (double)c.nx * c.ny * c.ldn * cs + 4.0 * items[i].slot_count * (double)c.nx * c.ny * cs;
+    }
   }
   prof->fronts = (int)sc->fronts.size();
   prof->items = (int)items.size();
@@ -535,6 +553,7 @@ lsw_status lsw_apply_precond_profiled(lsw_ctx* ctx, const void* x, void* y, int 
   prof->total_ms = tot;
   prof->alg_bytes = bytes;
   prof->alg_flops = flops;
+  prof->streamed_bytes = streamed;
   return LSW_OK;
 }
 

@@ -111,7 +111,7 @@ DevSlot blank_slot() {
 
 }  // namespace
 
-void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, int rmax, long long LP,
+void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const FrontPlan& plan, long long LP,
                     std::vector<Front>& fronts, std::vector<DevItem>& items, std::vector<DevSlot>& slots,
                     std::vector<DevGroup>& groups, long long n_dof2) {
   const int nc = (int)cells.size();
@@ -268,46 +268,99 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, int rmax
     fr.push_back(std::move(f));
   }
 
-  // ---- flatten into items (whole (shift, rhs) groups, at most rmax slots) ----
+  // ---- flatten into items ----
+  // An item takes whole (rhs, shift) groups while they fit in r slots; a
+  // group larger than r is split over items (its outputs are added
+  // atomically, so the split only costs an extra read of the factor).
+  auto flatten = [&](std::vector<SlotSpec>& v, int r, auto&& emit) {
+    size_t i = 0;
+    while (i < v.size()) {
+      std::vector<std::pair<size_t, size_t>> parts;
+      int count = 0;
+      while (i < v.size() && count < r) {
+        size_t j = i;
+        while (j < v.size() && v[j].rhs == v[i].rhs && v[j].shift == v[i].shift) ++j;
+        const int gsz = int(j - i);
+        if (count > 0 && count + gsz > r && gsz <= r) break;   // starts a fresh item whole
+        if (count + gsz > r) j = i + (r - count);
+        parts.emplace_back(i, j);
+        count += int(j - i);
+        i = j;
+      }
+      emit(parts, count);
+    }
+  };
   fronts.clear(); items.clear(); slots.clear(); groups.clear();
   for (auto& f : fr) {
-    Front F{(int)items.size(), 0, 0, 0};
+    for (auto& kv : f)
+      std::stable_sort(kv.second.begin(), kv.second.end(), [](const SlotSpec& a, const SlotSpec& b) {
+        return std::make_tuple(a.rhs, a.shift, a.order) < std::make_tuple(b.rhs, b.shift, b.order);
+      });
+    // choose the slots per item and the cluster size with the cost model
+    int ny_max = 1, nx_max = 1;
+    double fac_elems = 0.0;
+    for (auto& kv : f) {
+      ny_max = std::max(ny_max, cells[kv.first].ny);
+      nx_max = std::max(nx_max, cells[kv.first].nx);
+    }
+    int best_r = plan.rmax, best_cl = 1;
+    double best_t = 1e300;
+    long long best_items = 0;
+    for (int r : {16, 8, 4, 2, 1}) {
+      if (r > plan.rmax) continue;
+      long long n_items = 0;
+      int maxs = 0;
+      fac_elems = 0.0;
+      for (auto& kv : f) {
+        const DevCell& cl = cells[kv.first];
+        flatten(kv.second, r, [&](const std::vector<std::pair<size_t, size_t>>&, int count) {
+          ++n_items;
+          maxs = std::max(maxs, count);
+          fac_elems += 2.0 * cl.nx * (double)cl.ny * cl.ldn;
+        });
+      }
+      if (n_items == 0) continue;
+      const int R = front_rpad(maxs);
+      for (int cl = 1; cl <= plan.cluster_cap; cl *= 2) {
+        const int mc = std::max(1, plan.max_clusters[cl]);
+        if (plan.max_clusters[cl] <= 0 && cl > 1) continue;
+        const long long waves = (n_items + mc - 1) / mc;
+        const double line = plan.line_overhead + plan.slot_cost * R + plan.col_cost * ((ny_max + cl - 1) / cl) * R;
+        double t = (double)waves * (2.0 * nx_max - 1.0) * line;
+        t = std::max(t, fac_elems * plan.csize / plan.bytes_per_cycle);
+        // ties go to fewer items (less factor traffic), then to larger clusters
+        if (t < best_t * 0.98 || (t <= best_t * 1.02 && n_items < best_items)) {
+          best_t = t; best_r = r; best_cl = cl; best_items = n_items;
+        }
+      }
+    }
+    Front F{(int)items.size(), 0, 0, 0, best_cl};
     for (auto& kv : f) {
       const int c = kv.first;
       auto& v = kv.second;
-      std::stable_sort(v.begin(), v.end(), [](const SlotSpec& a, const SlotSpec& b) {
-        return std::make_tuple(a.rhs, a.shift, a.order) < std::make_tuple(b.rhs, b.shift, b.order);
-      });
-      size_t i = 0;
-      while (i < v.size()) {
+      const DevCell& cl = cells[c];
+      flatten(v, best_r, [&](const std::vector<std::pair<size_t, size_t>>& parts, int count) {
         DevItem it{};
         it.cell = c;
         it.slot_begin = (int)slots.size();
         it.group_begin = (int)groups.size();
-        while (i < v.size()) {
-          size_t j = i;
-          while (j < v.size() && v[j].rhs == v[i].rhs && v[j].shift == v[i].shift) ++j;
-          const int gsz = int(j - i);
-          if (gsz > rmax) throw std::runtime_error("sweep group larger than the slot capacity of a front item");
-          if (it.slot_count > 0 && it.slot_count + gsz > rmax) break;
+        for (auto& pr : parts) {
           DevGroup g{};
           g.slot_begin = (int)slots.size() - it.slot_begin;
-          g.slot_count = gsz;
-          g.shift = v[i].shift;
-          g.out_off = ((long long)v[i].rhs * 4 + v[i].shift) * n_dof2;
+          g.slot_count = int(pr.second - pr.first);
+          g.shift = v[pr.first].shift;
+          g.out_off = ((long long)v[pr.first].rhs * 4 + v[pr.first].shift) * n_dof2;
           groups.push_back(g);
-          for (size_t q = i; q < j; ++q) slots.push_back(v[q].s);
-          it.slot_count += gsz;
+          for (size_t q = pr.first; q < pr.second; ++q) slots.push_back(v[q].s);
           it.group_count++;
-          i = j;
         }
-        const DevCell& cl = cells[c];
+        it.slot_count = count;
         it.scratch_off = F.scratch_elems;
         F.scratch_elems += (long long)cl.nx * front_rpad(it.slot_count) * cl.ny;
         F.max_slots = std::max(F.max_slots, it.slot_count);
         items.push_back(it);
         F.item_count++;
-      }
+      });
     }
     fronts.push_back(F);
   }

@@ -93,6 +93,23 @@ struct Front {
   int item_begin, item_count;
   long long scratch_elems;
   int max_slots;
+  int cluster;            // CTAs per item chosen for this front
+};
+
+// What the front planner knows about the device: how many clusters of each
+// size (1, 2, 4, 8) are resident at once, and a per-line cost model of the
+// sweep-front kernel, fitted to clock traces of it on GB300 (cycles =
+// line_overhead + slot_cost x slots + col_cost x columns per CTA x slots),
+// with a bandwidth floor (factor bytes / bytes_per_cycle).
+struct FrontPlan {
+  int max_clusters[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  int cluster_cap = 8;
+  int rmax = 16;
+  int csize = 8;             // bytes per complex value of the factors
+  double line_overhead = 2500.0;
+  double slot_cost = 0.0;
+  double col_cost = 15.0;
+  double bytes_per_cycle = 3300.0;
 };
 
 struct Schedule {
@@ -107,7 +124,7 @@ struct Schedule {
 
 // Build the sweep schedule (stage 1, N-1 stage-2 fronts, 2N-3 stage-3 fronts,
 // all four shifted decompositions and nrhs right-hand sides in every front).
-void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, int rmax, long long LP,
+void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const FrontPlan& plan, long long LP,
                     std::vector<Front>& fronts, std::vector<DevItem>& items, std::vector<DevSlot>& slots,
                     std::vector<DevGroup>& groups, long long n_dof2);
 
@@ -151,6 +168,8 @@ inline int front_cluster(int items, int nsm) {
 }
 
 template <typename T> cudaError_t launch_front(const FrontArgs& a, int max_ny, int max_nx, cudaStream_t st);
+// clusters of `cluster` CTAs of the sweep-front kernel resident at once (one CTA per SM)
+int front_max_clusters(bool dbl, int cluster);
 int front_rmax(bool dbl);
 int front_rpad(int n);
 template <typename T> cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* prof,

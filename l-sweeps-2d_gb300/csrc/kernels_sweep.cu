@@ -770,6 +770,37 @@ cudaError_t launch_front(const FrontArgs& a_in, int max_ny, int max_nx, cudaStre
   return cudaLaunchKernelEx(&cfg, kern, a);
 }
 
+int front_max_clusters(bool dbl, int cluster) {
+  int dev = 0, maxopt = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaLaunchConfig_t cfg{};
+  cudaLaunchAttribute attr[1];
+  cfg.gridDim = dim3((unsigned)(cluster * 1024));
+  cfg.blockDim = dim3(32 * (kAux + kMaxRG * kMaxKSW));
+  cfg.dynamicSmemBytes = (size_t)maxopt;   // one CTA per SM, as every front launch
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  cudaError_t e;
+  if (dbl) {
+    cudaFuncSetAttribute(k_front<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
+    e = cudaOccupancyMaxActiveClusters(&n, k_front<double>, &cfg);
+  } else {
+    cudaFuncSetAttribute(k_front<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
+    e = cudaOccupancyMaxActiveClusters(&n, k_front<float>, &cfg);
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
 template cudaError_t launch_front<float>(const FrontArgs&, int, int, cudaStream_t);
 template cudaError_t launch_front<double>(const FrontArgs&, int, int, cudaStream_t);
 

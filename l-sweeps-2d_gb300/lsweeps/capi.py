@@ -39,7 +39,8 @@ class ProblemInfo(C.Structure):
 
 class ApplyProfile(C.Structure):
     _fields_ = [("fronts", C.c_int), ("items", C.c_int), ("slots", C.c_int), ("front_ms", C.c_double),
-                ("total_ms", C.c_double), ("alg_bytes", C.c_double), ("alg_flops", C.c_double)]
+                ("total_ms", C.c_double), ("alg_bytes", C.c_double), ("alg_flops", C.c_double),
+                ("streamed_bytes", C.c_double)]
 
 
 class CellInfo(C.Structure):
