@@ -11,6 +11,7 @@ built: no Eigen / libconfig++ / MPI)."""
 from __future__ import annotations
 
 import argparse
+import re
 import json
 import os
 import statistics
@@ -250,12 +251,10 @@ def run_gpu(args):
     peak, peak_kind = measured_peaks()
     achieved = pr["alg_bytes"] / (front_ms / 1e3) / 1e9
     traffic = None
-    tf = ROOT / "profiles" / "front_kernel_traffic.json"
+    tf = ROOT / "profiles" / "k_front_C2_dram_traffic.md"
     if tf.exists():
-        try:
-            traffic = json.loads(tf.read_text()).get("bytes_per_apply_c2")
-        except Exception:
-            traffic = None
+        m = re.search(r"traffic_bytes_per_apply_c2:\s*([0-9.eE+]+)", tf.read_text())
+        traffic = float(m.group(1)) if m else None
 
     # end to end through the host-buffer C call (H2D of b, D2H of x in the timed region)
     bh = torch.empty(S.n2, dtype=torch.complex128, pin_memory=True)

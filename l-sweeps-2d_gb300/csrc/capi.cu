@@ -150,7 +150,7 @@ lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out) {
       plan.cluster_cap = ctx->max_cluster;
       plan.rmax = front_rmax(dbl);
       plan.csize = dbl ? 16 : 8;
-      plan.col_cost = dbl ? 30.0 : 15.0;
+      if (dbl) { plan.col_cost = 40.0; plan.col_slot_cost = 20.0; }
       for (int cl = 1; cl <= 8; cl *= 2) plan.max_clusters[cl] = front_max_clusters(dbl, cl);
       if (plan.max_clusters[1] <= 0) plan.max_clusters[1] = ctx->nsm;
       build_schedule(ctx->cells, ctx->N, nrhs, plan, ctx->LP, sc->fronts, items, slots, groups, ctx->n2);

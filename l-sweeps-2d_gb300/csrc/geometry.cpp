@@ -325,7 +325,8 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
         const int mc = std::max(1, plan.max_clusters[cl]);
         if (plan.max_clusters[cl] <= 0 && cl > 1) continue;
         const long long waves = (n_items + mc - 1) / mc;
-        const double line = plan.line_overhead + plan.slot_cost * R + plan.col_cost * ((ny_max + cl - 1) / cl) * R;
+        const double line = plan.line_overhead + plan.slot_cost * R +
+                            (plan.col_cost + plan.col_slot_cost * R) * ((ny_max + cl - 1) / cl);
         double t = (double)waves * (2.0 * nx_max - 1.0) * line;
         t = std::max(t, fac_elems * plan.csize / plan.bytes_per_cycle);
         // ties go to fewer items (less factor traffic), then to larger clusters

@@ -98,17 +98,19 @@ struct Front {
 
 // What the front planner knows about the device: how many clusters of each
 // size (1, 2, 4, 8) are resident at once, and a per-line cost model of the
-// sweep-front kernel, fitted to clock traces of it on GB300 (cycles =
-// line_overhead + slot_cost x slots + col_cost x columns per CTA x slots),
+// sweep-front kernel fitted to front timings on GB300 over every (slots per
+// item, cluster size) choice of a C2 apply: cycles per line =
+//   line_overhead + slot_cost R + (col_cost + col_slot_cost R) x columns per CTA,
 // with a bandwidth floor (factor bytes / bytes_per_cycle).
 struct FrontPlan {
   int max_clusters[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   int cluster_cap = 8;
   int rmax = 16;
   int csize = 8;             // bytes per complex value of the factors
-  double line_overhead = 2500.0;
-  double slot_cost = 0.0;
-  double col_cost = 15.0;
+  double line_overhead = 1800.0;
+  double slot_cost = 250.0;
+  double col_cost = 25.0;
+  double col_slot_cost = 10.0;
   double bytes_per_cycle = 3300.0;
 };
 
