@@ -474,6 +474,7 @@ lsw_status lsw_factorize(lsw_ctx* ctx, void* stream) {
   int status = 0;
   CK(cudaMemcpyAsync(&status, ctx->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H status");
   CK(cudaStreamSynchronize(st), "factorize sync");
+  if (status & 6) return fail(ctx, LSW_ERR_CUDA, "factorisation kernel: cluster not formed or a bounded wait ran out");
   if (status & 1) return fail(ctx, LSW_ERR_SINGULAR_BLOCK, "zero or non-finite pivot in a Schur complement block");
   ctx->factorized = true;
   return LSW_OK;

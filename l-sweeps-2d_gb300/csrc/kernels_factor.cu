@@ -7,189 +7,471 @@
 // the neighbouring lines.  Block LU gives the Schur complements
 //   S_0 = D_0,   S_k = D_k - w_k e_{k-1} S_{k-1}^{-1},
 // and the factor kept for the solves is Sinv_k = S_k^{-1} for every line,
-// stored column-major (element (i, j) at j*ldn + i).  Each S_k is inverted by
-// Gauss-Jordan elimination with partial pivoting on unpivoted rows (implicit
-// row exchange, pivot order recorded), and the inverse is unscrambled on the
-// way out: Sinv[i][j] = W[piv[i]][pinv[j]].  One CTA per cell runs the whole
-// chain of lines; the working matrix sits in shared memory when it fits and
-// in a per-cell global (L2-resident) buffer otherwise.  A zero or non-finite
-// pivot sets bit 0 of *status (the reference exits on a failed factorisation,
-// LocalLinearSolverEigenSparseLU.cpp:54-58).
+// stored column-major (element (i, j) at j*ldn + i).
+//
+// Each S_k is inverted in place by Gauss-Jordan elimination with partial
+// pivoting on unpivoted rows (implicit row exchange, pivot order recorded;
+// the inverse is unscrambled on the way out: Sinv[i][j] = W[piv[i]][pinv[j]]),
+// blocked over B pivots (16 for complex64, 8 for complex128) so that the bulk of the work is a register-tiled
+// rank-B update instead of B passes over the whole matrix:
+//   * the panel (the B columns of the block) goes through the classic
+//     Gauss-Jordan steps; column t of the panel at its step, f_t, and the
+//     pivot p_t and 1/f_t[p_t] are recorded;
+//   * every other column c then receives all B steps at once:
+//       u_t = (c[p_t] - sum_{s<t} f_s[p_t] u_s) / f_t[p_t],
+//       c[r] -= sum_t f_t[r] u_t            (rows r that are not block pivots),
+//       c[p_t] = u_t - sum_{s>t} f_s[p_t] u_s,
+//     which is exactly the result of the B classic steps.
+//
+// One thread-block cluster of G CTAs works on a cell: CTA g holds the column
+// range [g n/G, (g+1) n/G) of the working matrix in shared memory (G = 2 for
+// complex64, 4 for complex128 at the C2-C4 cell sizes), the CTA owning a
+// panel publishes f_t, p_t and 1/f_t[p_t] through distributed shared memory,
+// and the cluster meets once per block on an mbarrier (bounded waits: a wait
+// that runs out sets bit 1 of *status and the CTA leaves).  A zero or
+// non-finite pivot sets bit 0 of *status (the reference exits on a failed
+// factorisation, LocalLinearSolverEigenSparseLU.cpp:54-58).
 #include "common.cuh"
 #include "internal.h"
+
+#include <algorithm>
 
 namespace lsw {
 
 namespace {
 
-constexpr int kFT = 1024;
-constexpr int kHdr = 12 * 1024;  // pivot buffers, flags and reduction scratch (11.7 KB used)
+constexpr int kFT = 512;              // threads per CTA
+constexpr int kTX = 16, kTY = 32;     // update tile grid (columns x rows)
+constexpr int kRI = 6;                // rows per thread in the update: ny <= 192
+constexpr int kMaxN = kRI * kTY;
+constexpr long long kWaitCycles = 4000000000LL;   // ~2 s at 2 GHz
+constexpr unsigned kSuspendNs = 1000000;
+
+template <typename T> struct FacCfg;
+// CJ: columns per thread in the update tile; B: pivots per block
+template <> struct FacCfg<float> { static constexpr int CJ = 6, B = 16; };
+template <> struct FacCfg<double> { static constexpr int CJ = 3, B = 8; };
+
+__device__ __forceinline__ unsigned saddr(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned cluster_size() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned mapa(unsigned a, unsigned rank) {
+  unsigned r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_remote(uint64_t* b, unsigned rank) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(mapa(saddr(b), rank))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t* b, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(saddr(b)), "r"(parity), "r"(kSuspendNs)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ float2 ld_remote(const float2* p, unsigned rank) {
+  float2 v;
+  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(mapa(saddr(p), rank))
+               : "memory");
+  return v;
+}
+__device__ __forceinline__ double2 ld_remote(const double2* p, unsigned rank) {
+  double2 v;
+  asm volatile("ld.shared::cluster.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "r"(mapa(saddr(p), rank))
+               : "memory");
+  return v;
+}
+__device__ __forceinline__ void named_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+__device__ __forceinline__ int ld_remote(const int* p, unsigned rank) {
+  int v;
+  asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(mapa(saddr(p), rank)) : "memory");
+  return v;
+}
+
+// block-column owner: CTA g owns the columns [g n/G, (g+1) n/G)
+__device__ __forceinline__ int col_owner(int j, int n, int G) { return ((j + 1) * G - 1) / n; }
 
 template <typename T>
 __global__ void __launch_bounds__(kFT, 1)
 k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
             const double* __restrict__ mgrid, int n_dof, double omega2, cx_t<T>* __restrict__ fac,
-            cx_t<T>* __restrict__ work, long long work_stride, int use_smem, int* status) {
+            int G, int nmax, int ldw, int* status) {
   using C = cx_t<T>;
+  constexpr int CJ = FacCfg<T>::CJ;
+  constexpr int kB = FacCfg<T>::B;
   extern __shared__ __align__(16) unsigned char smem[];
-  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
-  const DevCell cl = cells[blockIdx.x];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const unsigned g = G > 1 ? cluster_rank() : 0u;
+  if (G > 1 && (cluster_size() != (unsigned)G || g != blockIdx.x % (unsigned)G)) {
+    if (tid == 0) atomicOr(status, 4);   // the launch did not form the expected clusters
+    return;
+  }
+  const DevCell cl = cells[blockIdx.x / G];
   const int n = cl.ny, nx = cl.nx, ldn = cl.ldn;
-  const int ldw = n;
+  const int c0 = (int)g * n / G, c1 = ((int)g + 1) * n / G, nc = c1 - c0;
 
-  C* colbuf = reinterpret_cast<C*>(smem);
-  C* rowbuf = colbuf + 256;
-  int* used = reinterpret_cast<int*>(rowbuf + 256);
-  int* piv = used + 256;
-  int* pinv = piv + 256;
-  T* wbest = reinterpret_cast<T*>(pinv + 256);
-  int* wbi = reinterpret_cast<int*>(wbest + 32);
-  int* sp = wbi + 32;
-  C* W = use_smem ? reinterpret_cast<C*>(smem + kHdr) : work + (long long)blockIdx.x * work_stride;
+  // ---- shared layout (identical in every CTA of the cluster) ----
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 8);
+  int* sp = reinterpret_cast<int*>(smem + 12);
+  T* wbest = reinterpret_cast<T*>(smem + 16);                 // [16]
+  int* wbi = reinterpret_cast<int*>(smem + 16 + 16 * 8);      // [16]
+  int* used = reinterpret_cast<int*>(smem + 256);             // [nmax]
+  int* piv = used + kMaxN;                                     // [nmax]
+  int* pslot = piv + kMaxN;                                    // [nmax] block pivot slot of a row, -1 if none
+  int* pb = pslot + kMaxN;                                     // [2][kB]
+  C* invv = reinterpret_cast<C*>(pb + 2 * kB);                 // [2][kB]
+  C* rowp = invv + 2 * kB;                                     // [kB]
+  C* M1 = rowp + kB;                                           // [kB][kB]
+  C* F = M1 + kB * kB;                                         // [2][kB][nmax]
+  C* U = F + 2 * kB * nmax;                                    // [kB][ldw]
+  C* W = U + kB * ldw;                                         // [nmax][ldw], my columns
 
   const double2* px = prof + cl.prof_off;  // lo_x, hi_x, dg_x, lo_y, hi_y, dg_y
   const double2* py = px + 3 * nx;
-  C* F = fac + cl.fac_off;
+  C* Fac = fac + cl.fac_off;
   const C z = czero<C>();
 
+  if (tid == 0) {
+    *abort_flag = 0;
+    mbar_init(bar, (unsigned)G);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int i = tid; i < kMaxN; i += kFT) pslot[i] = -1;
+  __syncthreads();
+  if (G > 1) asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+
+  // cluster-wide barrier: every CTA's thread t < G arrives on CTA t's
+  // mbarrier (release after the CTA barrier, so it covers every thread's
+  // writes), then every thread waits for its own CTA's phase (acquire)
+  unsigned phase = 0;
+  auto csync = [&]() -> bool {
+    __syncthreads();
+    if (G == 1) return true;
+    if (tid < G) mbar_arrive_remote(bar, (unsigned)tid);
+    bool ok = mbar_try_wait_cluster(bar, phase & 1u);
+    if (!ok) {
+      const long long t0 = clock64();
+      while (!(ok = mbar_try_wait_cluster(bar, phase & 1u))) {
+        if (*abort_flag) break;
+        if (clock64() - t0 > kWaitCycles) {
+          *abort_flag = 1;
+          atomicOr(status, 2);
+          break;
+        }
+      }
+    }
+    ++phase;
+    __syncthreads();
+    return *abort_flag == 0;
+  };
+
   for (int k = 0; k < nx; ++k) {
-    // ---- Schur complement S_k into W (row-major) ----
+    // ---- Schur complement S_k, my columns, into W (row-major) ----
     const C dgx = to_c(px[2 * nx + k], z);
     C coup = z;
     if (k > 0) coup = cmul(to_c(px[k], z), to_c(px[nx + k - 1], z));   // w_k e_{k-1}
-    const C* Fp = F + (size_t)(k - 1) * n * ldn;
+    const C* Fp = Fac + (size_t)(k - 1) * n * ldn;
     const double* mrow = mgrid + (long long)(cl.lox + k) * n_dof + cl.loy;
-    for (int i = ty; i < n; i += 32) {
-      for (int j = tx; j < n; j += 32) {
-        C v = z;
-        if (k > 0) v = cneg(cmul(coup, Fp[(size_t)j * ldn + i]));
-        if (j == i) {
-          C d = cadd(dgx, to_c(py[2 * n + i], z));
-          d.x -= (T)(omega2 * mrow[i]);
-          v = cadd(v, d);
-        } else if (j == i - 1) {
-          v = cadd(v, to_c(py[i], z));          // coupling to j-1 (south)
-        } else if (j == i + 1) {
-          v = cadd(v, to_c(py[n + i], z));      // coupling to j+1 (north)
-        }
-        W[(size_t)i * ldw + j] = v;
+    for (int e = tid; e < n * nc; e += kFT) {
+      const int cc = e / n, i = e - cc * n, j = c0 + cc;
+      C v = z;
+      if (k > 0) v = cneg(cmul(coup, Fp[(size_t)j * ldn + i]));
+      if (j == i) {
+        C d = cadd(dgx, to_c(py[2 * n + i], z));
+        d.x -= (T)(omega2 * mrow[i]);
+        v = cadd(v, d);
+      } else if (j == i - 1) {
+        v = cadd(v, to_c(py[i], z));          // coupling to j-1 (south)
+      } else if (j == i + 1) {
+        v = cadd(v, to_c(py[n + i], z));      // coupling to j+1 (north)
       }
+      W[(size_t)i * ldw + cc] = v;
     }
     for (int i = tid; i < n; i += kFT) used[i] = 0;
     __syncthreads();
 
-    // ---- Gauss-Jordan inversion in place ----
-    for (int kk = 0; kk < n; ++kk) {
-      T best = (T)-1; int bi = n;
-      for (int r = tid; r < n; r += kFT) {
-        const C v = W[(size_t)r * ldw + kk];
-        colbuf[r] = v;
-        if (!used[r]) {
-          const T a2 = abs2(v);
-          if (a2 > best) { best = a2; bi = r; }
-        }
-      }
+    // ---- blocked Gauss-Jordan over the pivot columns in order ----
+    int blk = 0;
+    for (int k0 = 0; k0 < n; ++blk) {
+      const int o = col_owner(k0, n, G);
+      const int oend = (o + 1) * n / G;
+      const int k1 = min(k0 + kB, oend), bt = k1 - k0, buf = blk & 1;
+      C* Fb = F + (size_t)buf * kB * nmax;
+      int* pbb = pb + buf * kB;
+      C* ivb = invv + buf * kB;
+
+      if ((int)g == o && tid < kMaxN) {
+        // panel: the classic steps on columns [k0, k1) of my W, one row per
+        // thread of the first kMaxN / 32 warps, the row's panel part in
+        // registers (named barrier 1 among those warps)
+        const int r = tid;
+        const bool live = r < n;
+        const int pc = k0 - c0;
+        C row[kB];
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const T ob = __shfl_down_sync(0xffffffffu, best, off);
-        const int oi = __shfl_down_sync(0xffffffffu, bi, off);
-        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-      }
-      if (tx == 0) { wbest[ty] = best; wbi[ty] = bi; }
-      __syncthreads();
-      if (ty == 0) {
-        best = wbest[tx]; bi = wbi[tx];
+        for (int q = 0; q < kB; ++q) row[q] = (live && q < bt) ? W[(size_t)r * ldw + pc + q] : z;
+        bool mine_used = live ? (used[r] != 0) : true;
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-          const T ob = __shfl_down_sync(0xffffffffu, best, off);
-          const int oi = __shfl_down_sync(0xffffffffu, bi, off);
-          if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-        }
-        if (tx == 0) {
+        for (int t = 0; t < kB; ++t) {
+          if (t >= bt) break;
+          const C v = row[t];
+          if (live) Fb[(size_t)t * nmax + r] = v;
+          T best = (live && !mine_used) ? abs2(v) : (T)-1;
+          int bi = (live && !mine_used) ? r : n;
+#pragma unroll
+          for (int off = 16; off > 0; off >>= 1) {
+            const T ob = __shfl_down_sync(0xffffffffu, best, off);
+            const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+          }
+          if (lane == 0) { wbest[warp] = best; wbi[warp] = bi; }
+          named_sync(1, kMaxN);
+          best = wbest[0];
+          bi = wbi[0];
+#pragma unroll
+          for (int w = 1; w < kMaxN / 32; ++w) {
+            const T ob = wbest[w];
+            const int oi = wbi[w];
+            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+          }
           if (!(best > (T)0) || !isfinite((double)best) || bi >= n) {
-            atomicOr(status, 1);
+            if (r == 0) atomicOr(status, 1);
             // keep going with the first unpivoted row so the kernel terminates normally
             bi = 0;
             while (bi < n && used[bi]) ++bi;
             if (bi >= n) bi = 0;
           }
-          sp[0] = bi;
-          used[bi] = 1;
-          piv[kk] = bi;
-        }
-      }
-      __syncthreads();
-      const int p = sp[0];
-      const C inv = crcp(colbuf[p]);
-      for (int j = tid; j < n; j += kFT) rowbuf[j] = (j == kk) ? inv : cmul(W[(size_t)p * ldw + j], inv);
-      __syncthreads();
-      for (int r = ty; r < n; r += 32) {
-        C* Wr = W + (size_t)r * ldw;
-        if (r == p) {
-          for (int j = tx; j < n; j += 32) Wr[j] = rowbuf[j];
-        } else {
-          const C f = colbuf[r];
-          for (int j = tx; j < n; j += 32) {
-            if (j == kk) {
-              Wr[j] = cneg(cmul(f, rowbuf[kk]));
-            } else {
-              C w = Wr[j];
-              cfms(w, f, rowbuf[j]);
-              Wr[j] = w;
+          const int p = bi;
+          if (r == p) {
+            const C inv = crcp(v);
+            mine_used = true;
+            used[r] = 1;
+            piv[k0 + t] = r;
+            pbb[t] = r;
+            ivb[t] = inv;
+#pragma unroll
+            for (int q = 0; q < kB; ++q) {
+              if (q < bt) {
+                row[q] = (q == t) ? inv : cmul(row[q], inv);
+                rowp[q] = row[q];
+              }
             }
+          }
+          named_sync(1, kMaxN);
+          if (live && r != p) {
+            const C inv = ivb[t];
+#pragma unroll
+            for (int q = 0; q < kB; ++q) {
+              if (q < bt) {
+                if (q == t) row[q] = cneg(cmul(v, inv));
+                else cfms(row[q], v, rowp[q]);
+              }
+            }
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < kB; ++q)
+          if (live && q < bt) W[(size_t)r * ldw + pc + q] = row[q];
+      }
+      if (!csync()) return;
+      if ((int)g != o) {
+        // the panel owner's columns f_t, pivots and reciprocals
+        for (int e = tid; e < bt * n; e += kFT) {
+          const int t = e / n, r = e - t * n;
+          Fb[(size_t)t * nmax + r] = ld_remote(Fb + (size_t)t * nmax + r, (unsigned)o);
+        }
+        if (tid < bt) {
+          const int p = ld_remote(pbb + tid, (unsigned)o);
+          pbb[tid] = p;
+          ivb[tid] = ld_remote(ivb + tid, (unsigned)o);
+          used[p] = 1;
+          piv[k0 + tid] = p;
+        }
+        __syncthreads();
+      }
+      if (tid < bt) pslot[pbb[tid]] = tid;
+      __syncthreads();
+
+      // (a) u = M1 g per column, with M1 = (D + L)^{-1} (D = diag f_t[p_t],
+      // L[t][s] = f_s[p_t], s < t) formed once per block by one warp, lane j
+      // solving for column j; then the pivot rows' final values
+      // c[p_t] = u_t - sum_{s>t} f_s[p_t] u_s
+      const int pk0 = ((int)g == o) ? k0 - c0 : -1;   // my panel columns [pk0, pk0 + bt), if any
+      if (warp == 0 && lane < bt) {
+        C m[kB];
+#pragma unroll
+        for (int t = 0; t < kB; ++t) {
+          if (t < bt) {
+            C a = (t == lane) ? to_c(make_double2(1.0, 0.0), z) : z;
+#pragma unroll
+            for (int s2 = 0; s2 < kB; ++s2)
+              if (s2 < t) cfms(a, Fb[(size_t)s2 * nmax + pbb[t]], m[s2]);
+            m[t] = cmul(a, ivb[t]);
+            M1[t * kB + lane] = m[t];
           }
         }
       }
       __syncthreads();
+      for (int e = tid; e < bt * nc; e += kFT) {
+        const int t = e / nc, cc = e - t * nc;
+        if (pk0 >= 0 && cc >= pk0 && cc < pk0 + bt) continue;
+        C a = z;
+        for (int s2 = 0; s2 <= t; ++s2) cfma(a, M1[t * kB + s2], W[(size_t)pbb[s2] * ldw + cc]);
+        U[(size_t)t * ldw + cc] = a;
+      }
+      __syncthreads();
+      for (int e = tid; e < bt * nc; e += kFT) {
+        const int t = e / nc, cc = e - t * nc;
+        if (pk0 >= 0 && cc >= pk0 && cc < pk0 + bt) continue;
+        C a = U[(size_t)t * ldw + cc];
+        const int pt = pbb[t];
+        for (int s2 = t + 1; s2 < bt; ++s2) cfms(a, Fb[(size_t)s2 * nmax + pt], U[(size_t)s2 * ldw + cc]);
+        W[(size_t)pt * ldw + cc] = a;
+      }
+      __syncthreads();
+
+      // (b) rank-bt update of the other rows: c[r] -= sum_t f_t[r] u_t
+      {
+        const int tx = tid % kTX, ty = tid / kTX;
+        C acc[kRI][CJ];
+#pragma unroll
+        for (int a = 0; a < kRI; ++a)
+#pragma unroll
+          for (int b = 0; b < CJ; ++b) acc[a][b] = z;
+        for (int t = 0; t < bt; ++t) {
+          C fr[kRI], uc[CJ];
+#pragma unroll
+          for (int a = 0; a < kRI; ++a) {
+            const int r = ty + kTY * a;
+            fr[a] = r < n ? Fb[(size_t)t * nmax + r] : z;
+          }
+#pragma unroll
+          for (int b = 0; b < CJ; ++b) {
+            const int cc = tx + kTX * b;
+            uc[b] = cc < nc ? U[(size_t)t * ldw + cc] : z;
+          }
+#pragma unroll
+          for (int a = 0; a < kRI; ++a)
+#pragma unroll
+            for (int b = 0; b < CJ; ++b) cfma(acc[a][b], fr[a], uc[b]);
+        }
+#pragma unroll
+        for (int a = 0; a < kRI; ++a) {
+          const int r = ty + kTY * a;
+          if (r >= n || pslot[r] >= 0) continue;
+#pragma unroll
+          for (int b = 0; b < CJ; ++b) {
+            const int cc = tx + kTX * b;
+            if (cc >= nc || (pk0 >= 0 && cc >= pk0 && cc < pk0 + bt)) continue;
+            C* w = W + (size_t)r * ldw + cc;
+            *w = csub(*w, acc[a][b]);
+          }
+        }
+      }
+      __syncthreads();
+      if (tid < bt) pslot[pbb[tid]] = -1;
+      __syncthreads();
+      k0 = k1;
     }
 
-    // ---- unscramble into the factor pool (column-major, zero padding) ----
-    for (int i = tid; i < n; i += kFT) pinv[piv[i]] = i;
-    __syncthreads();
-    C* Fk = F + (size_t)k * n * ldn;
-    for (int e = tid; e < n * ldn; e += kFT) {
-      const int j = e / ldn, i = e - j * ldn;
-      Fk[e] = (i < n) ? W[(size_t)piv[i] * ldw + pinv[j]] : z;
+    // ---- unscramble my columns: output column piv[c] holds W[piv[i]][c] ----
+    C* Fk = Fac + (size_t)k * n * ldn;
+    for (int e = tid; e < nc * ldn; e += kFT) {
+      const int cc = e / ldn, i = e - cc * ldn;
+      const int j = piv[c0 + cc];
+      Fk[(size_t)j * ldn + i] = (i < n) ? W[(size_t)piv[i] * ldw + cc] : z;
     }
-    __syncthreads();
+    // the next line's Schur complement reads every CTA's columns of Sinv_k
+    if (!csync()) return;
   }
+}
+
+template <typename T>
+size_t fac_smem(int nmax, int ldw) {
+  using C = cx_t<T>;
+  constexpr int kB = FacCfg<T>::B;
+  return 256 + 3 * (size_t)kMaxN * sizeof(int) + 2 * kB * sizeof(int) + (3 * kB + kB * kB) * sizeof(C) +
+         2 * (size_t)kB * nmax * sizeof(C) + (size_t)kB * ldw * sizeof(C) + (size_t)nmax * ldw * sizeof(C);
+}
+
+// smallest cluster whose column slices fit the update tiles and shared memory
+template <typename T>
+int fac_cluster(int nmax, int maxopt, int* ldw_out) {
+  for (int G = 1; G <= 8; G *= 2) {
+    const int ldw = (nmax + G - 1) / G;
+    if (ldw > kTX * FacCfg<T>::CJ) continue;
+    if (fac_smem<T>(nmax, ldw) <= (size_t)maxopt) {
+      *ldw_out = ldw;
+      return G;
+    }
+  }
+  return 0;
 }
 
 }  // namespace
 
 size_t factor_smem_bytes(int ny, bool dbl) {
-  const size_t cs = dbl ? 16 : 8;
-  return kHdr + (size_t)ny * ny * cs;
+  int dev = 0, maxopt = 0, ldw = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const int G = dbl ? fac_cluster<double>(ny, maxopt, &ldw) : fac_cluster<float>(ny, maxopt, &ldw);
+  if (G == 0) return 0;
+  return dbl ? fac_smem<double>(ny, ldw) : fac_smem<float>(ny, ldw);
 }
 
 template <typename T>
 cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* prof, const double* mgrid,
-                             int n_dof, double omega2, void* fac, void* work, int max_ny, int* status,
+                             int n_dof, double omega2, void* fac, void* /*work*/, int max_ny, int* status,
                              cudaStream_t st) {
   if (ncell <= 0) return cudaSuccess;
-  const bool dbl = sizeof(T) == 8;
-  size_t smem = factor_smem_bytes(max_ny, dbl);
-  int dev = 0, maxopt = 0;
+  if (max_ny > kMaxN) return cudaErrorInvalidValue;
+  int dev = 0, maxopt = 0, ldw = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const int use_smem = smem <= (size_t)maxopt ? 1 : 0;
-  if (!use_smem) smem = kHdr;
-  if (!use_smem && work == nullptr) return cudaErrorInvalidValue;
+  const int G = fac_cluster<T>(max_ny, maxopt, &ldw);
+  if (G == 0) return cudaErrorInvalidConfiguration;
+  const size_t smem = fac_smem<T>(max_ny, ldw);
   auto kern = k_factorize<T>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  kern<<<ncell, kFT, smem, st>>>(cells, prof, mgrid, n_dof, omega2, reinterpret_cast<cx_t<T>*>(fac),
-                                 reinterpret_cast<cx_t<T>*>(work), (long long)max_ny * max_ny, use_smem,
-                                 status);
-  return cudaGetLastError();
+  cudaLaunchConfig_t cfg{};
+  cudaLaunchAttribute attr[1];
+  cfg.gridDim = dim3((unsigned)(ncell * G));
+  cfg.blockDim = dim3(kFT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)G;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, cells, prof, mgrid, n_dof, omega2, reinterpret_cast<cx_t<T>*>(fac), G,
+                            max_ny, ldw, status);
 }
 
-bool factor_needs_work(int max_ny, bool dbl) {
-  int dev = 0, maxopt = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  return factor_smem_bytes(max_ny, dbl) > (size_t)maxopt;
-}
+bool factor_needs_work(int, bool) { return false; }
 
 template cudaError_t launch_factorize<float>(const DevCell*, int, const double2*, const double*, int, double,
                                              void*, void*, int, int*, cudaStream_t);
