@@ -352,6 +352,31 @@ def run_apply_only(args):
                       "applies": args.warmup + args.steps, "fronts_per_apply": 3 * spec.N - 3 + 1}))
 
 
+def run_serve(args):
+    """Serving stream (grids 256^2-2048^2 of 128^2 cells, 6-10 points per
+    wavelength, lens/layered media with 30 % repeats, 1-16 sources, Poisson
+    arrivals): one JSON line per arrival rate with p50/p99 latency and
+    solves/s.  The stream is a scaled-down instance (`--serve-requests`) of
+    the 2,000-request workload."""
+    from lsweeps.serving import GpuBackend, ServeEngine, serving_stream
+    rates = [float(r) for r in args.serve_rates.split(",")]
+    for i, rate in enumerate(rates):
+        # every rate starts from an empty factor cache with its own stream
+        eng = ServeEngine(GpuBackend(0), slots=args.serve_slots, max_batch=8)
+        reqs = serving_stream(args.serve_requests, rate_hz=rate, seed=3 + i)
+        st = eng.run(reqs, realtime=True)
+        res = [r.true_rel_res for r in reqs if r.error is None]
+        print(json.dumps({"metric": "serving: p50/p99 latency and solves/s at rel. residual 1e-6",
+                          "rate_hz": rate, "requests": len(reqs), "unit": "solves/s",
+                          "value": st.solves_per_s, **st.as_dict(),
+                          "max_true_rel_res": max(res) if res else None,
+                          "config": {"workload": "serving stream: grids {256,512,1024,2048}^2 of 128^2 cells, "
+                                                 "6-10 ppw, lens/layered media with 30% repeats, 1-16 sources, "
+                                                 "Poisson arrivals", "precision": "mixed", "slots": args.serve_slots,
+                                     "max_batch": 8}}), flush=True)
+        eng.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -365,10 +390,17 @@ def main():
     ap.add_argument("--ref-budget", type=float, default=15.0)
     ap.add_argument("--ref-iterations", type=int, default=14)
     ap.add_argument("--apply-only", action="store_true", help="only preconditioner applies (profiling workload)")
+    ap.add_argument("--serve", action="store_true", help="serving stream at the rates of --serve-rates")
+    ap.add_argument("--serve-rates", default="1,4,16")
+    ap.add_argument("--serve-requests", type=int, default=40)
+    ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--config", default="C2")
     ap.add_argument("--precision", default="c64")
     ap.add_argument("--nrhs", type=int, default=1)
     args = ap.parse_args()
+    if args.serve:
+        run_serve(args)
+        return
     if args.apply_only:
         run_apply_only(args)
     elif args.impl == "reference":

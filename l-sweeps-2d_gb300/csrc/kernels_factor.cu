@@ -453,7 +453,9 @@ cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* pro
   if (G == 0) return cudaErrorInvalidConfiguration;
   const size_t smem = fac_smem<T>(max_ny, ldw);
   auto kern = k_factorize<T>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // the attribute is an upper bound: always the device maximum, so that
+  // host threads launching concurrently never lower it under one another
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg{};
   cudaLaunchAttribute attr[1];

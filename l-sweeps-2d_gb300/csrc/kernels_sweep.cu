@@ -764,7 +764,9 @@ cudaError_t launch_front(const FrontArgs& a_in, int max_ny, int max_nx, cudaStre
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   auto kern = k_front<T>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // the attribute is an upper bound: always the device maximum, so that
+  // host threads launching concurrently never lower it under one another
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
   if (e != cudaSuccess) return e;
   cfg.blockDim = dim3(32 * (kAux + kMaxRG * kMaxKSW));
   return cudaLaunchKernelEx(&cfg, kern, a);
