@@ -1,5 +1,7 @@
-"""Build liblsweeps_gb300.so in-tree: every translation unit of csrc/ compiled
-for sm_103a in parallel with nvcc, linked with the static CUDA runtime."""
+"""Build liblsweeps_gb300.so in-tree: every translation unit of csrc/ (the
+kernels and the C ABI) and host/ (the C++ classes of the reference's plugin
+API) compiled for sm_103a in parallel with nvcc and linked with the static
+CUDA runtime, plus the driver executable lsweeps_gb300_main."""
 from __future__ import annotations
 
 import concurrent.futures as cf
@@ -12,6 +14,8 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent
 CSRC = HERE / "csrc"
+HOST = HERE / "host"
+MAIN = HERE / "lsweeps" / "lsweeps_gb300_main"
 OUT_DIR = HERE / "_build"
 LIB = HERE / "lsweeps" / "liblsweeps_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -33,7 +37,7 @@ def _flags(verbose_ptxas: bool) -> list[str]:
 
 
 def _compile(src: Path, verbose_ptxas: bool) -> tuple[Path, str]:
-    obj = OUT_DIR / (src.stem + ".o")
+    obj = OUT_DIR / ((src.parent.name + "_") + src.stem + ".o")
     cmd = [nvcc(), "-c", str(src), "-o", str(obj)] + _flags(verbose_ptxas)
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -43,9 +47,12 @@ def _compile(src: Path, verbose_ptxas: bool) -> tuple[Path, str]:
 
 def build(verbose_ptxas: bool = False, force: bool = False) -> Path:
     srcs = sorted(list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cpp")))
-    deps = srcs + sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + [ROOT / "include" / "lsweeps.h"]
-    if LIB.exists() and not force and not verbose_ptxas:
-        t = LIB.stat().st_mtime
+    srcs += [HOST / "host.cpp", HOST / "input.cpp"]
+    deps = srcs + sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + [ROOT / "include" / "lsweeps.h",
+                                                                          ROOT / "include" / "lsweeps_host.hpp",
+                                                                          HOST / "main.cpp"]
+    if LIB.exists() and MAIN.exists() and not force and not verbose_ptxas:
+        t = min(LIB.stat().st_mtime, MAIN.stat().st_mtime)
         if all(d.stat().st_mtime <= t for d in deps):
             return LIB
     OUT_DIR.mkdir(exist_ok=True)
@@ -61,6 +68,14 @@ def build(verbose_ptxas: bool = False, force: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    # the reference's driver (main.cpp) over the library
+    tmpm = MAIN.with_suffix(".tmp")
+    cmd = [nvcc(), str(HOST / "main.cpp"), "-o", str(tmpm), "-std=c++17", "-O2", f"-I{ROOT / 'include'}",
+           f"-L{LIB.parent}", "-llsweeps_gb300", "-Xlinker", "-rpath=$ORIGIN"] + ARCH
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmpm, MAIN)
     return LIB
 
 
