@@ -28,8 +28,18 @@ for _p in (ROOT, ROOT / "l-sweeps-2d_gb300"):
 
 METRIC = "time-to-solution & solves/s at rel. residual 1e-6: mixed vs FP64 on GB300; p50/p99"
 UNIT = "solves/s"
-WORKLOAD = ("C2: 2D Helmholtz, 1031^2 elements (1062^2 DOFs with PML), Gaussian lens c=1-0.4exp(-r^2/0.02), "
-            "8 ppw at c_min, 8x8 checkerboard of 128^2 cells, PML 16, 1 point source, FGMRES(30) tol 1e-6")
+WORKLOADS = {
+    "C1": "C1: 2D Helmholtz, 259^2 elements, c = 1, 10 ppw, 4x4 checkerboard of 64^2 cells, PML 10, "
+          "1 point source, FGMRES(30) tol 1e-6",
+    "C2": "C2: 2D Helmholtz, 1031^2 elements (1062^2 DOFs with PML), Gaussian lens c=1-0.4exp(-r^2/0.02), "
+          "8 ppw at c_min, 8x8 checkerboard of 128^2 cells, PML 16, 1 point source, FGMRES(30) tol 1e-6",
+    "C3": "C3: 2D Helmholtz, 2063^2 elements, 12 seeded layers c in [1.5,4.5] + 5% smoothed perturbation, "
+          "8 ppw, 16x16 checkerboard of 128^2 cells, PML 20, 64 sources on a line solved as one batch of "
+          "64 right-hand sides, FGMRES(30) tol 1e-6",
+    "C4": "C4: 2D Helmholtz, 4127^2 elements, seeded piecewise-smooth c in [1.5,5.0] (sigma 8 cells), "
+          "8 ppw at c_min, 32x32 checkerboard of 128^2 cells, PML 20, 1 centred source, FGMRES(30) tol 1e-6",
+}
+WORKLOAD = WORKLOADS["C2"]
 
 
 def pctl(v, q):
@@ -197,7 +207,8 @@ def run_gpu(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    spec, med = config("C2")
+    spec, med = config(args.config)
+    WORKLOAD = WORKLOADS[args.config.upper()]
     S = Solver(spec, med, precision="c64", device=local)
     st = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -206,7 +217,12 @@ def run_gpu(args):
     e1.record(st)
     torch.cuda.synchronize()
     fact_s = e0.elapsed_time(e1) / 1e3
-    b = S.assemble_rhs(spec.sources)
+    if args.config.upper() == "C3":
+        # one right-hand side per source, solved as one batch
+        b = torch.cat([S.assemble_rhs([src]) for src in spec.sources])
+    else:
+        b = S.assemble_rhs(spec.sources)
+    nrhs = b.numel() // S.n2
     x = torch.empty_like(b)
 
     def solve():
@@ -238,11 +254,11 @@ def run_gpu(args):
         t = torch.tensor([dev_total], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         dev_total = float(t.item())
-    value = world * args.steps / dev_total
+    value = world * args.steps * nrhs / dev_total   # right-hand sides solved per second
 
     # roofline of the dominant kernel (sweep fronts) from CUDA events
     prof_runs = []
-    v = torch.randn(S.n2, dtype=torch.complex128, device=dev)
+    v = torch.randn(S.n2 * nrhs, dtype=torch.complex128, device=dev)
     for _ in range(3):
         _, pr = S.apply_precond_profiled(v)
         prof_runs.append(pr)
@@ -252,7 +268,7 @@ def run_gpu(args):
     achieved = pr["alg_bytes"] / (front_ms / 1e3) / 1e9
     traffic = None
     tf = ROOT / "profiles" / "k_front_C2_dram_traffic.md"
-    if tf.exists():
+    if tf.exists() and args.config.upper() == "C2" and nrhs == 1:
         m = re.search(r"traffic_bytes_per_apply_c2:\s*([0-9.eE+]+)", tf.read_text())
         traffic = float(m.group(1)) if m else None
 
@@ -268,7 +284,7 @@ def run_gpu(args):
         t = time.perf_counter()
         xh, rep_h = S.solve_host(bnp, tol=args.tol, max_iter=300, restart=30)
         te.append(time.perf_counter() - t)
-    e2e_value = world * len(te) / sum(te)
+    e2e_value = world * len(te) * nrhs / sum(te)
 
     # plain FP64 GPU path
     S64 = None
@@ -305,10 +321,14 @@ def run_gpu(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_total * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64 factors/applies + f64 Krylov",
-            "data": "synthetic (seeded Gaussian-lens medium)",
+            "data": {"C1": "synthetic (constant medium)", "C2": "synthetic (seeded Gaussian-lens medium)",
+                     "C3": "synthetic (seeded layered medium)",
+                     "C4": "synthetic (seeded piecewise-smooth random medium)"}[args.config.upper()],
             "config": {"workload": WORKLOAD, "precision": "mixed", "restart": 30, "tol": args.tol,
                        "parallelism": f"replicas x{world}",
-                       "l2": "inputs larger than L2: 2.3 GB of c64 factors streamed per apply (L2 129 MB)"},
+                       "nrhs": nrhs,
+                       "l2": f"inputs larger than L2: {S.info()['factor_bytes'] / 1e9:.1f} GB of c64 factors "
+                             "streamed per apply (L2 129 MB)"},
             "p50_ms": p50, "p99_ms": pctl(step_ms, 0.99), "iterations": reps[-1].iterations,
             "true_rel_res": reps[-1].true_rel_res, "factorize_s": fact_s,
             "time_to_solution_s": fact_s + p50 / 1e3,
@@ -324,8 +344,8 @@ def run_gpu(args):
                          "front_ms_per_apply": front_ms, "fronts": pr["fronts"], "items": pr["items"],
                          "slots": pr["slots"], "apply_ms": pr["total_ms"]},
             "cpu_baseline": cpu,
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": S.n2 * 16,
-                    "d2h_bytes_per_step": S.n2 * 16, "steps": len(te)},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": S.n2 * 16 * nrhs,
+                    "d2h_bytes_per_step": S.n2 * 16 * nrhs, "steps": len(te)},
             "clocks": clocks,
             "gpu_launches": gpu_launches,
             "wall_s_timed": elapsed,
