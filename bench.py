@@ -40,6 +40,12 @@ WORKLOADS = {
           "8 ppw at c_min, 32x32 checkerboard of 128^2 cells, PML 20, 1 centred source, FGMRES(30) tol 1e-6",
 }
 WORKLOAD = WORKLOADS["C2"]
+# factor and sweep arithmetic per workload: complex FP32 where the workload names it, the
+# BF16-split tensor-core products (hi + lo bf16 terms, FP32 accumulation) for the 4096^2 case
+PRECISION = {"C1": "c64", "C2": "c64", "C3": "c64", "C4": "bf16x2"}
+DTYPE = {"c64": "c64 factors/applies + f64 Krylov",
+         "bf16x2": "bf16-split factor products (hi+lo, fp32 accumulate) + f64 Krylov",
+         "c128": "c128 factors/applies + f64 Krylov"}
 
 
 def pctl(v, q):
@@ -209,7 +215,8 @@ def run_gpu(args):
 
     spec, med = config(args.config)
     WORKLOAD = WORKLOADS[args.config.upper()]
-    S = Solver(spec, med, precision="c64", device=local)
+    prec = args.precision or PRECISION[args.config.upper()]
+    S = Solver(spec, med, precision=prec, device=local)
     st = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(st)
@@ -320,14 +327,15 @@ def run_gpu(args):
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_total * 1e3 / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c64 factors/applies + f64 Krylov",
+            "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[prec],
             "data": {"C1": "synthetic (constant medium)", "C2": "synthetic (seeded Gaussian-lens medium)",
                      "C3": "synthetic (seeded layered medium)",
                      "C4": "synthetic (seeded piecewise-smooth random medium)"}[args.config.upper()],
-            "config": {"workload": WORKLOAD, "precision": "mixed", "restart": 30, "tol": args.tol,
+            "config": {"workload": WORKLOAD, "precision": "mixed" if prec != "c128" else "fp64",
+                       "factor_precision": prec, "restart": 30, "tol": args.tol,
                        "parallelism": f"replicas x{world}",
                        "nrhs": nrhs,
-                       "l2": f"inputs larger than L2: {S.info()['factor_bytes'] / 1e9:.1f} GB of c64 factors "
+                       "l2": f"inputs larger than L2: {S.info()['factor_bytes'] / 1e9:.1f} GB of {prec} factors "
                              "streamed per apply (L2 129 MB)"},
             "p50_ms": p50, "p99_ms": pctl(step_ms, 0.99), "iterations": reps[-1].iterations,
             "true_rel_res": reps[-1].true_rel_res, "factorize_s": fact_s,
@@ -362,13 +370,14 @@ def run_apply_only(args):
     from lsweeps.problems import config
     from lsweeps.solver import Solver
     spec, med = config(args.config)
-    S = Solver(spec, med, precision=args.precision)
+    prec = args.precision or PRECISION[args.config.upper()]
+    S = Solver(spec, med, precision=prec)
     S.factorize()
     v = torch.randn(S.n2 * args.nrhs, dtype=torch.complex128, device="cuda")
     for _ in range(args.warmup + args.steps):
         S.apply_precond(v)
     torch.cuda.synchronize()
-    print(json.dumps({"apply_only": args.config, "precision": args.precision, "nrhs": args.nrhs,
+    print(json.dumps({"apply_only": args.config, "precision": prec, "nrhs": args.nrhs,
                       "applies": args.warmup + args.steps, "fronts_per_apply": 3 * spec.N - 3 + 1}))
 
 
@@ -415,7 +424,8 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=40)
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--config", default="C2")
-    ap.add_argument("--precision", default="c64")
+    ap.add_argument("--precision", default=None, choices=["c64", "bf16x2", "c128"],
+                    help="factor/sweep arithmetic (default: the workload's, c64 for C1-C3, bf16x2 for C4)")
     ap.add_argument("--nrhs", type=int, default=1)
     args = ap.parse_args()
     if args.serve:

@@ -51,7 +51,11 @@ typedef enum lsw_status {
  * matvec, Krylov vectors, Arnoldi and Hessenberg work are always FP64. */
 typedef enum lsw_precision {
   LSW_PREC_C128 = 0, /* complex double factors and applies (reference arithmetic) */
-  LSW_PREC_C64 = 1   /* complex float factors and applies, FP32 accumulation */
+  LSW_PREC_C64 = 1,  /* complex float factors and applies, FP32 accumulation */
+  LSW_PREC_SPLIT = 2 /* complex float applies whose factor products run on the tensor cores:
+                        every factor entry stored as two bf16 terms (hi + lo, 8 bytes per
+                        complex value like complex float), three bf16 products per entry
+                        (hi*hi + hi*lo + lo*hi) accumulated in FP32 */
 } lsw_precision;
 
 typedef enum lsw_gmres_mode {

@@ -17,7 +17,6 @@
 #include <vector>
 
 namespace lsw {
-bool factor_needs_work(int max_ny, bool dbl);
 }
 
 using namespace lsw;
@@ -94,16 +93,22 @@ lsw_status cuda_fail(lsw_ctx* c, cudaError_t e, const char* where) {
     ctx->launches += (n);       \
   } while (0)
 
-inline size_t csize(int prec) { return prec == LSW_PREC_C64 ? 8 : 16; }
+inline size_t csize(int prec) { return prec == LSW_PREC_C128 ? 16 : 8; }
 inline cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
-DevCell make_cell(int I, int J, int N, int m, int p) {
+DevCell make_cell(int I, int J, int N, int m, int p, bool split) {
   DevCell c{};
   const DirGeom gx = dir_geom(J, N, m, p), gy = dir_geom(I, N, m, p);
   c.I = I; c.J = J;
   c.nx = gx.nd; c.ny = gy.nd;
   c.lox = gx.lo; c.loy = gy.lo;
   c.ldn = (gy.nd + 3) & ~3;
+  // bf16-split factors: a column stride of 4 (mod 8) complex values keeps the
+  // four columns of an mma A fragment in distinct shared-memory banks
+  if (split) {
+    c.ldn = gy.nd;
+    while (c.ldn % 8 != 4) ++c.ldn;
+  }
   for (int s = 0; s < 2; ++s) {
     for (int l = 0; l < 4; ++l) { c.lx[s][l] = gx.lines[s][l]; c.ly[s][l] = gy.lines[s][l]; }
     c.ownx[s][0] = gx.own[s][0]; c.ownx[s][1] = gx.own[s][1];
@@ -151,6 +156,10 @@ lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out) {
       plan.rmax = front_rmax(dbl);
       plan.csize = dbl ? 16 : 8;
       if (dbl) { plan.col_cost = 40.0; plan.col_slot_cost = 20.0; }
+      if (ctx->prec == LSW_PREC_SPLIT) {
+        // tensor-core matvec: the per-column cost hardly grows with the slots
+        plan.line_overhead = 2200.0; plan.slot_cost = 0.0; plan.col_cost = 40.0; plan.col_slot_cost = 3.0;
+      }
       for (int cl = 1; cl <= 8; cl *= 2) plan.max_clusters[cl] = front_max_clusters(dbl, cl);
       if (plan.max_clusters[1] <= 0) plan.max_clusters[1] = ctx->nsm;
       build_schedule(ctx->cells, ctx->N, nrhs, plan, ctx->LP, sc->fronts, items, slots, groups, ctx->n2);
@@ -201,6 +210,7 @@ lsw_status precond_impl(lsw_ctx* ctx, const double2* x, double2* y, int nrhs, cu
   a.x_stride = ctx->n2;
   a.n_dof = ctx->n_dof; a.N = ctx->N; a.m = ctx->m; a.p = ctx->p;
   a.err = ctx->d_status.as<int>() + 1;
+  a.split = ctx->prec == LSW_PREC_SPLIT ? 1 : 0;
   for (size_t fi = 0; fi < sc->fronts.size(); ++fi) {
     const Front& f = sc->fronts[fi];
     a.items = sc->d_items + f.item_begin;
@@ -208,15 +218,15 @@ lsw_status precond_impl(lsw_ctx* ctx, const double2* x, double2* y, int nrhs, cu
     a.max_slots = f.max_slots;
     a.cluster = f.cluster;
     if (ctx->front_events) CK(cudaEventRecord((*ctx->front_events)[2 * fi], st), "event");
-    cudaError_t e = ctx->prec == LSW_PREC_C64 ? launch_front<float>(a, ctx->max_ny, ctx->max_nx, st)
-                                              : launch_front<double>(a, ctx->max_ny, ctx->max_nx, st);
+    cudaError_t e = ctx->prec != LSW_PREC_C128 ? launch_front<float>(a, ctx->max_ny, ctx->max_nx, st)
+                                               : launch_front<double>(a, ctx->max_ny, ctx->max_nx, st);
     CK(e, "front kernel");
     if (ctx->front_events) CK(cudaEventRecord((*ctx->front_events)[2 * fi + 1], st), "event");
     ctx->launches += f.item_count > 0 ? 1 : 0;
   }
   ctx->launches += 1;
-  cudaError_t e = ctx->prec == LSW_PREC_C64 ? launch_combine<float>(ctx->d_outs.p, y, nrhs, ctx->n2, st)
-                                            : launch_combine<double>(ctx->d_outs.p, y, nrhs, ctx->n2, st);
+  cudaError_t e = ctx->prec != LSW_PREC_C128 ? launch_combine<float>(ctx->d_outs.p, y, nrhs, ctx->n2, st)
+                                             : launch_combine<double>(ctx->d_outs.p, y, nrhs, ctx->n2, st);
   CK(e, "combine kernel");
   return LSW_OK;
 }
@@ -368,7 +378,7 @@ lsw_status lsw_geometry_cell(const lsw_geom* g, int cell, lsw_cell_info* out) {
   if (!out || !geom_valid(g, &why)) return LSW_ERR_INVALID_ARGUMENT;
   const int N = g->n_cells;
   if (cell < 0 || cell >= N * N) return LSW_ERR_INVALID_ARGUMENT;
-  fill_info(make_cell(cell / N, cell % N, N, g->n_els_in_cell, g->pml), out);
+  fill_info(make_cell(cell / N, cell % N, N, g->n_els_in_cell, g->pml, false), out);
   return LSW_OK;
 }
 
@@ -379,7 +389,7 @@ lsw_status lsw_problem_setup(lsw_ctx* ctx, const lsw_geom* g, const double* m_gr
   if (!m_grid) return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "m_grid is NULL");
   if (!(omega > 1.0) || !std::isfinite(omega))
     return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "omega must be > 1 (PML absorption C = ln omega must be positive)");
-  if (precision != LSW_PREC_C128 && precision != LSW_PREC_C64)
+  if (precision != LSW_PREC_C128 && precision != LSW_PREC_C64 && precision != LSW_PREC_SPLIT)
     return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "unknown precision");
   CK(cudaSetDevice(ctx->device), "cudaSetDevice");
   // drop everything of a previous problem
@@ -400,7 +410,7 @@ lsw_status lsw_problem_setup(lsw_ctx* ctx, const lsw_geom* g, const double* m_gr
   ctx->max_nx = ctx->max_ny = 0;
   for (int I = 0; I < ctx->N; ++I)
     for (int J = 0; J < ctx->N; ++J) {
-      DevCell c = make_cell(I, J, ctx->N, ctx->m, ctx->p);
+      DevCell c = make_cell(I, J, ctx->N, ctx->m, ctx->p, precision == LSW_PREC_SPLIT);
       c.fac_off = fac_off;
       fac_off += (long long)c.nx * c.ny * c.ldn;
       c.prof_off = (long long)prof.size();
@@ -421,9 +431,10 @@ lsw_status lsw_problem_setup(lsw_ctx* ctx, const lsw_geom* g, const double* m_gr
   CK(ctx->d_m.ensure((size_t)ctx->n2 * sizeof(double)), "cudaMalloc(m)");
   CK(ctx->d_fac.ensure((size_t)fac_off * cs), "cudaMalloc(factors)");
   CK(ctx->d_status.ensure(16), "cudaMalloc(status)");
-  const bool dbl = precision == LSW_PREC_C128;
-  if (factor_needs_work(ctx->max_ny, dbl)) {
-    CK(ctx->d_work.ensure((size_t)ctx->ncell * ctx->max_ny * ctx->max_ny * cs), "cudaMalloc(factor work)");
+  if (precision == LSW_PREC_SPLIT) {
+    // each cell's previous FP32 Schur-complement inverse, for the recurrence
+    CK(ctx->d_work.ensure((size_t)ctx->ncell * ctx->max_ny * (ctx->max_ny + 8) * sizeof(float2)),
+       "cudaMalloc(factor work)");
   }
   CK(cudaMemcpy(ctx->d_cells.p, ctx->cells.data(), ctx->cells.size() * sizeof(DevCell), cudaMemcpyHostToDevice), "H2D cells");
   CK(cudaMemcpy(ctx->d_prof.p, prof.data(), prof.size() * sizeof(double2), cudaMemcpyHostToDevice), "H2D prof");
@@ -463,10 +474,10 @@ lsw_status lsw_factorize(lsw_ctx* ctx, void* stream) {
   CK(cudaMemsetAsync(ctx->d_status.p, 0, 16, st), "memset status");
   ctx->launches += 1;
   const double w2 = ctx->omega * ctx->omega;
-  cudaError_t e = ctx->prec == LSW_PREC_C64
+  cudaError_t e = ctx->prec != LSW_PREC_C128
                       ? launch_factorize<float>(ctx->d_cells.as<DevCell>(), ctx->ncell, ctx->d_prof.as<double2>(),
                                                 ctx->d_m.as<double>(), ctx->n_dof, w2, ctx->d_fac.p, ctx->d_work.p,
-                                                ctx->max_ny, ctx->d_status.as<int>(), st)
+                                                ctx->max_ny, ctx->d_status.as<int>(), st, ctx->prec == LSW_PREC_SPLIT)
                       : launch_factorize<double>(ctx->d_cells.as<DevCell>(), ctx->ncell, ctx->d_prof.as<double2>(),
                                                  ctx->d_m.as<double>(), ctx->n_dof, w2, ctx->d_fac.p, ctx->d_work.p,
                                                  ctx->max_ny, ctx->d_status.as<int>(), st);
@@ -632,6 +643,7 @@ lsw_status lsw_local_solve(lsw_ctx* ctx, int cell, const void* b, void* x, int n
   a.item_count = (int)items.size();
   a.max_slots = std::min(rmax, nrhs);
   a.err = ctx->d_status.as<int>() + 1;
+  a.split = ctx->prec == LSW_PREC_SPLIT ? 1 : 0;
   a.cluster = std::min(ctx->max_cluster, front_cluster(a.item_count, ctx->nsm));
   cudaError_t e = dbl ? launch_front<double>(a, ctx->max_ny, ctx->max_nx, st) : launch_front<float>(a, ctx->max_ny, ctx->max_nx, st);
   CK(e, "local solve kernel");
@@ -1052,6 +1064,7 @@ lsw_status lsw_local_solve_noalloc(lsw_ctx* ctx, int cell, const void* b, void* 
   a.item_count = n_items;
   a.max_slots = std::min(rmax, nrhs);
   a.err = ctx->d_status.as<int>() + 1;
+  a.split = ctx->prec == LSW_PREC_SPLIT ? 1 : 0;
   a.cluster = std::min(ctx->max_cluster, front_cluster(a.item_count, ctx->nsm));
   cudaError_t e = dbl ? launch_front<double>(a, ctx->max_ny, ctx->max_nx, st) : launch_front<float>(a, ctx->max_ny, ctx->max_nx, st);
   CK(e, "local solve kernel");

@@ -161,6 +161,7 @@ struct FrontArgs {
   int stages;             // shared-memory ring depth (set by the launcher)
   int chunk;              // factor columns per streamed chunk (set by the launcher)
   int ksw;                // consumer column slices (set by the launcher)
+  int split;              // factors hold bf16 hi/lo terms; the matvec runs on mma.sync
 };
 // CTAs per item for a front of `items` cell solves on `nsm` SMs
 inline int front_cluster(int items, int nsm) {
@@ -174,10 +175,12 @@ template <typename T> cudaError_t launch_front(const FrontArgs& a, int max_ny, i
 int front_max_clusters(bool dbl, int cluster);
 int front_rmax(bool dbl);
 int front_rpad(int n);
+// split: write every factor entry as bf16 hi/lo terms; `prev` then holds each
+// cell's previous FP32 block (ny x ldn complex per cell) for the Schur recurrence
 template <typename T> cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* prof,
                                                    const double* mgrid, int n_dof, double omega2,
-                                                   void* fac, void* work, int max_ny, int* status,
-                                                   cudaStream_t st);
+                                                   void* fac, void* prev, int max_ny, int* status,
+                                                   cudaStream_t st, bool split = false);
 size_t factor_smem_bytes(int ny, bool dbl);
 
 cudaError_t launch_apply_A(const double2* x, double2* y, int nrhs, int n_dof, const double2* gprof,

@@ -34,6 +34,8 @@
 #include "common.cuh"
 #include "internal.h"
 
+#include <cuda_bf16.h>
+
 #include <algorithm>
 
 namespace lsw {
@@ -108,6 +110,21 @@ __device__ __forceinline__ int ld_remote(const int* p, unsigned rank) {
   return v;
 }
 
+// bf16 hi/lo terms of x: hi = rn(x), lo = rn(x - hi)
+__device__ __forceinline__ void bf16_split(float x, unsigned& hi, unsigned& lo) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(x);
+  const __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
+  hi = (unsigned)__bfloat16_as_ushort(h);
+  lo = (unsigned)__bfloat16_as_ushort(l);
+}
+// one factor entry of the split layout: {hi(re) | hi(im) << 16, lo(re) | lo(im) << 16}
+__device__ __forceinline__ uint2 split_entry(float2 v) {
+  unsigned hr, lr, hi_, li;
+  bf16_split(v.x, hr, lr);
+  bf16_split(v.y, hi_, li);
+  return make_uint2(hr | (hi_ << 16), lr | (li << 16));
+}
+
 // block-column owner: CTA g owns the columns [g n/G, (g+1) n/G)
 __device__ __forceinline__ int col_owner(int j, int n, int G) { return ((j + 1) * G - 1) / n; }
 
@@ -115,7 +132,7 @@ template <typename T>
 __global__ void __launch_bounds__(kFT, 1)
 k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
             const double* __restrict__ mgrid, int n_dof, double omega2, cx_t<T>* __restrict__ fac,
-            int G, int nmax, int ldw, int* status) {
+            cx_t<T>* __restrict__ prev, long long prev_stride, int split, int G, int nmax, int ldw, int* status) {
   using C = cx_t<T>;
   constexpr int CJ = FacCfg<T>::CJ;
   constexpr int kB = FacCfg<T>::B;
@@ -150,6 +167,7 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
   const double2* px = prof + cl.prof_off;  // lo_x, hi_x, dg_x, lo_y, hi_y, dg_y
   const double2* py = px + 3 * nx;
   C* Fac = fac + cl.fac_off;
+  C* Prev = prev ? prev + (long long)(blockIdx.x / G) * prev_stride : nullptr;   // split: Sinv_{k-1} in FP32
   const C z = czero<C>();
 
   if (tid == 0) {
@@ -191,7 +209,7 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
     const C dgx = to_c(px[2 * nx + k], z);
     C coup = z;
     if (k > 0) coup = cmul(to_c(px[k], z), to_c(px[nx + k - 1], z));   // w_k e_{k-1}
-    const C* Fp = Fac + (size_t)(k - 1) * n * ldn;
+    const C* Fp = split ? Prev : Fac + (size_t)(k - 1) * n * ldn;
     const double* mrow = mgrid + (long long)(cl.lox + k) * n_dof + cl.loy;
     for (int e = tid; e < n * nc; e += kFT) {
       const int cc = e / n, i = e - cc * n, j = c0 + cc;
@@ -400,7 +418,15 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
     for (int e = tid; e < nc * ldn; e += kFT) {
       const int cc = e / ldn, i = e - cc * ldn;
       const int j = piv[c0 + cc];
-      Fk[(size_t)j * ldn + i] = (i < n) ? W[(size_t)piv[i] * ldw + cc] : z;
+      const C v = (i < n) ? W[(size_t)piv[i] * ldw + cc] : z;
+      if constexpr (sizeof(T) == 4) {
+        if (split) {
+          Prev[(size_t)j * ldn + i] = v;
+          reinterpret_cast<uint2*>(Fk)[(size_t)j * ldn + i] = split_entry(v);
+          continue;
+        }
+      }
+      Fk[(size_t)j * ldn + i] = v;
     }
     // the next line's Schur complement reads every CTA's columns of Sinv_k
     if (!csync()) return;
@@ -442,8 +468,8 @@ size_t factor_smem_bytes(int ny, bool dbl) {
 
 template <typename T>
 cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* prof, const double* mgrid,
-                             int n_dof, double omega2, void* fac, void* /*work*/, int max_ny, int* status,
-                             cudaStream_t st) {
+                             int n_dof, double omega2, void* fac, void* prev, int max_ny, int* status,
+                             cudaStream_t st, bool split) {
   if (ncell <= 0) return cudaSuccess;
   if (max_ny > kMaxN) return cudaErrorInvalidValue;
   int dev = 0, maxopt = 0, ldw = 0;
@@ -469,15 +495,18 @@ cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* pro
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kern, cells, prof, mgrid, n_dof, omega2, reinterpret_cast<cx_t<T>*>(fac), G,
+  if (split && (sizeof(T) != 4 || prev == nullptr)) return cudaErrorInvalidValue;
+  // previous-block buffer: max_ny x ldn_max complex per cell (ldn_max <= max_ny + 7)
+  const long long prev_stride = (long long)max_ny * (max_ny + 8);
+  return cudaLaunchKernelEx(&cfg, kern, cells, prof, mgrid, n_dof, omega2, reinterpret_cast<cx_t<T>*>(fac),
+                            reinterpret_cast<cx_t<T>*>(split ? prev : nullptr), prev_stride, split ? 1 : 0, G,
                             max_ny, ldw, status);
 }
 
-bool factor_needs_work(int, bool) { return false; }
 
 template cudaError_t launch_factorize<float>(const DevCell*, int, const double2*, const double*, int, double,
-                                             void*, void*, int, int*, cudaStream_t);
+                                             void*, void*, int, int*, cudaStream_t, bool);
 template cudaError_t launch_factorize<double>(const DevCell*, int, const double2*, const double*, int, double,
-                                              void*, void*, int, int*, cudaStream_t);
+                                              void*, void*, int, int*, cudaStream_t, bool);
 
 }  // namespace lsw

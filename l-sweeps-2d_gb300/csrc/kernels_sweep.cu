@@ -48,6 +48,8 @@
 #include "common.cuh"
 #include "internal.h"
 
+#include <cuda_bf16.h>
+
 #include <algorithm>
 
 namespace lsw {
@@ -172,6 +174,23 @@ __device__ __forceinline__ void red_add(double2* p, double2 v) {
   atomicAdd(&p->y, v.y);
 }
 
+// bf16x2 words of the hi and lo terms of (a, b): low half a, high half b
+__device__ __forceinline__ void split_pair(float a, float b, unsigned& hi, unsigned& lo) {
+  const __nv_bfloat16 ah = __float2bfloat16_rn(a), bh = __float2bfloat16_rn(b);
+  const __nv_bfloat16 al = __float2bfloat16_rn(a - __bfloat162float(ah));
+  const __nv_bfloat16 bl = __float2bfloat16_rn(b - __bfloat162float(bh));
+  hi = (unsigned)__bfloat16_as_ushort(ah) | ((unsigned)__bfloat16_as_ushort(bh) << 16);
+  lo = (unsigned)__bfloat16_as_ushort(al) | ((unsigned)__bfloat16_as_ushort(bl) << 16);
+}
+// D += A B, m16n8k16, bf16 operands, FP32 accumulation
+__device__ __forceinline__ void mma_bf16(float (&d)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
+                                         unsigned b0, unsigned b1) {
+  asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+               "{%0,%1,%2,%3};"
+               : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+               : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
 // CTA c of a cluster of CL owns rows/columns [c*ny/CL, (c+1)*ny/CL)
 __device__ __forceinline__ int owner_of(int row, int ny, int CL) { return ((row + 1) * CL - 1) / ny; }
 
@@ -255,7 +274,7 @@ template <> struct Pair<double> {
   __device__ __forceinline__ void load(const double2* p) { a = p[0]; b = p[1]; }
 };
 
-template <typename T, int R>
+template <typename T, int R, bool SPLIT>
 __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it, const DevCell& cl, unsigned char* smem) {
   using C = cx_t<T>;
   const int CW = a.chunk;              // columns per chunk, multiple of 8
@@ -275,7 +294,10 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   const int jb = (int)crank * ny / CL, je = ((int)crank + 1) * ny / CL;
   const int nJ = je - jb;               // my columns / rows of every line
   const int RG = (ny + 63) >> 6;        // row groups of 64 rows
-  const int NCW = KSW * RG;             // consumer warps
+  // consumer warps: KSW column slices per row group, or (split) one per 16-row m-tile
+  const int NCW = SPLIT ? (ny + 15) >> 4 : KSW * RG;
+  constexpr int NT = (2 * R + 7) / 8;   // split: n-tiles of 8 (Re, Im interleaved per slot)
+  constexpr int NT8 = NT * 8;
   const int NCT = NCW * 32;
   const int NSYNC = NCT + 96;           // consumers + 2 helper warps + writer warp
   const int nch = (nJ + CW - 1) / CW;   // chunks per line
@@ -319,7 +341,13 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   const size_t qbuf = (size_t)CL * qplane;
   p = al16(p + 2 * qbuf * sizeof(C));
   C* LS = reinterpret_cast<C*>(p);      // [KSW][R][64 RG] the column slices' partial sums, before their sum
-  p = al16(p + (size_t)KSW * 64 * RG * R * sizeof(C));
+  if (!SPLIT) p = al16(p + (size_t)KSW * 64 * RG * R * sizeof(C));
+  // split: the next line's input as mma B words, hi and lo terms, [column][n]
+  // with n = 2 slot + (0: real part, 1: imaginary part) of the product
+  const int nJ8 = ((nJcap + 7) & ~7) + 8;
+  unsigned* BwH = reinterpret_cast<unsigned*>(p);
+  unsigned* BwL = BwH + (size_t)nJ8 * NT8;
+  if (SPLIT) p = al16(p + 2 * (size_t)nJ8 * NT8 * sizeof(unsigned));
   int* rowinfo = reinterpret_cast<int*>(p);   // [ny] owner CTA << 16 | row offset in the owner's range
   p = al16(p + sizeof(int) * ny);
   DevSlot* sl = reinterpret_cast<DevSlot*>(p);
@@ -374,6 +402,13 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   for (int k = tid; k < nx; k += blockDim.x) {
     wsh[k] = to_c(px[k], czero<C>());
     esh[k] = to_c(px[nx + k], czero<C>());
+  }
+  if constexpr (SPLIT) {
+    // the mma k-steps of a chunk's last columns and rows past ldn read ring
+    // entries no copy wrote; zeros (with zero B words past my columns) keep
+    // them finite and without effect
+    for (size_t i = tid; i < (size_t)NS * slot_elems; i += blockDim.x) ring[i] = czero<C>();
+    for (size_t i = tid; i < 2 * (size_t)nJ8 * NT8; i += blockDim.x) BwH[i] = 0u;
   }
   if (tid == 0) {
     *abort_flag = 0;
@@ -563,10 +598,28 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   const int r0 = rg * 64 + 2 * lane;    // my row pair
   const bool rows_ok = r0 < ldn;
 
+  // split: the mma B words of input entry e = (column, slot) of the next line,
+  // n = 2 slot: (re, -im), n = 2 slot + 1: (im, re), hi and lo terms
+  auto write_bw = [&](int e, C v) {
+    if constexpr (SPLIT) {
+      const int jj = e / R, r = e - jj * R;
+      unsigned h0, l0, h1, l1;
+      split_pair(v.x, -v.y, h0, l0);
+      split_pair(v.y, v.x, h1, l1);
+      BwH[(size_t)jj * NT8 + 2 * r] = h0;
+      BwL[(size_t)jj * NT8 + 2 * r] = l0;
+      BwH[(size_t)jj * NT8 + 2 * r + 1] = h1;
+      BwL[(size_t)jj * NT8 + 2 * r + 1] = l1;
+    }
+  };
+
   prologue(ct);
   named_sync(1, NSYNC);       // every b_k is in scratch
   named_sync(1, NSYNC);       // S0
-  for (int e = ct; e < R * nJ; e += NCT) V[e] = H[e];
+  for (int e = ct; e < R * nJ; e += NCT) {
+    V[e] = H[e];
+    write_bw(e, H[e]);
+  }
   named_sync(1, NSYNC);       // S0b
 
   // bytes of partial sums that land in my Q per line: my rows x R x CL CTAs
@@ -581,68 +634,123 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
     // previous sync2 (peers' bytes may land before this; the phase cannot
     // complete without this arrive)
     if (CL > 1 && ct == 0 && li + 1 < nline) mbar_expect_tx(&pready[(li + 1) & 1], line_bytes);
-    // ---- partial products of my row pair with my slice of my columns ----
-    C acc0[R], acc1[R];
+    C* Qb = Q + buf * qbuf;
+    if constexpr (SPLIT) {
+      // ---- tensor-core partial products: my 16-row m-tile with all my columns ----
+      // A (factor, bf16 hi/lo words, column-major) x B (next input, [column][n])
+      // on mma.sync m16n8k16: three products hi*hi + hi*lo + lo*hi per k-step
+      float cacc[NT][4];
 #pragma unroll
-    for (int r = 0; r < R; ++r) { acc0[r] = czero<C>(); acc1[r] = czero<C>(); }
-    for (int c = 0; c < nch; ++c, ++idx) {
-      const int slot = (int)(idx % NS);
-      const bool ok = mbar_wait<false>(&full[slot], (unsigned)((idx / NS) & 1), a.err, abort_flag);
-      const C* S = ring + (size_t)slot * slot_elems + r0;
-      const int c0 = c * CW;
-      const int ncol = min(CW, nJ - c0);
-      if (ok && rows_ok) {
-#pragma unroll 2
-        for (int cc = ks; cc < ncol; cc += KSW) {
-          Pair<T> s;
-          s.load(S + (size_t)cc * ldn);
-          const C* v = V + (size_t)(c0 + cc) * R;
+      for (int nt = 0; nt < NT; ++nt) cacc[nt][0] = cacc[nt][1] = cacc[nt][2] = cacc[nt][3] = 0.f;
+      const int g = lane >> 2, t = lane & 3, mb = cw * 16;
+      for (int c = 0; c < nch; ++c, ++idx) {
+        const int slot = (int)(idx % NS);
+        const bool ok = mbar_wait<false>(&full[slot], (unsigned)((idx / NS) & 1), a.err, abort_flag);
+        const uint2* S2 = reinterpret_cast<const uint2*>(ring + (size_t)slot * slot_elems) + mb + g;
+        const int c0 = c * CW;
+        const int nks = (min(CW, nJ - c0) + 7) >> 3;
+        if (ok) {
+          for (int kq = 0; kq < nks; ++kq) {
+            const uint2* pa = S2 + (size_t)(kq * 8 + t) * ldn;
+            const uint2 e0 = pa[0], e1 = pa[8], e2 = pa[4 * (size_t)ldn], e3 = pa[4 * (size_t)ldn + 8];
+            const size_t bo = (size_t)(c0 + kq * 8 + t) * NT8 + g;
 #pragma unroll
-          for (int r = 0; r < R; ++r) {
-            const C vr = v[r];
-            cfma(acc0[r], s.a, vr);
-            cfma(acc1[r], s.b, vr);
+            for (int nt = 0; nt < NT; ++nt) {
+              const unsigned bh0 = BwH[bo + nt * 8], bh1 = BwH[bo + 4 * NT8 + nt * 8];
+              const unsigned bl0 = BwL[bo + nt * 8], bl1 = BwL[bo + 4 * NT8 + nt * 8];
+              mma_bf16(cacc[nt], e0.x, e1.x, e2.x, e3.x, bh0, bh1);
+              mma_bf16(cacc[nt], e0.x, e1.x, e2.x, e3.x, bl0, bl1);
+              mma_bf16(cacc[nt], e0.y, e1.y, e2.y, e3.y, bh0, bh1);
+            }
+          }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[slot]);
+      }
+      // lane (g, t) holds slot nt*4 + t (real, imaginary) of rows mb+g and mb+g+8:
+      // push each to the CTA that owns the row
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt) {
+        const int sidx = nt * 4 + t;
+        if (sidx < R) {
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int row = mb + g + 8 * h;
+            if (row < ny) {
+              C v;
+              v.x = cacc[nt][2 * h];
+              v.y = cacc[nt][2 * h + 1];
+              const int info = rowinfo[row];
+              C* dst = Qb + ((size_t)crank * nJcap + (info & 0xffff)) * R + sidx;
+              if (CL == 1) *dst = v;
+              else st_async(dst, (unsigned)(info >> 16), v, &pready[buf]);
+            }
           }
         }
       }
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&empty[slot]);
-    }
-    // sum the row group's column slices in shared memory, then push each
-    // row's sum to the CTA that owns the row
-    // (rows fastest: a lane's row pair is one 16-byte store per slot for
-    // float, and consecutive lanes hit consecutive banks)
-    const int RG64 = 64 * RG;
-    {
-      C* ls = LS + (size_t)ks * R * RG64 + r0;
-#pragma unroll
-      for (int r = 0; r < R; ++r) { ls[(size_t)r * RG64] = acc0[r]; ls[(size_t)r * RG64 + 1] = acc1[r]; }
-    }
-    named_sync(3 + rg, KSW * 32);
-    C* Qb = Q + buf * qbuf;
-    {
-      constexpr int UP = (sizeof(T) == 4 && R % 2 == 0) ? 2 : 1;   // slots per store
-      constexpr int NU = R / UP;                                  // stores per row
-      const size_t lsplane = (size_t)R * RG64;
-      for (int u = ks * 32 + lane; u < 64 * NU; u += KSW * 32) {
-        const int up = u >> 6, rr = u & 63;   // consecutive lanes take consecutive rows
-        const int row = rg * 64 + rr;
-        if (row >= ny) continue;
-        const C* src = LS + (size_t)up * UP * RG64 + row;
-        C v0 = src[0], v1 = UP == 2 ? src[RG64] : czero<C>();
-        for (int q = 1; q < KSW; ++q) {
-          v0 = cadd(v0, src[q * lsplane]);
-          if (UP == 2) v1 = cadd(v1, src[q * lsplane + RG64]);
+    } else {
+      // ---- partial products of my row pair with my slice of my columns ----
+      C acc0[R], acc1[R];
+  #pragma unroll
+      for (int r = 0; r < R; ++r) { acc0[r] = czero<C>(); acc1[r] = czero<C>(); }
+      for (int c = 0; c < nch; ++c, ++idx) {
+        const int slot = (int)(idx % NS);
+        const bool ok = mbar_wait<false>(&full[slot], (unsigned)((idx / NS) & 1), a.err, abort_flag);
+        const C* S = ring + (size_t)slot * slot_elems + r0;
+        const int c0 = c * CW;
+        const int ncol = min(CW, nJ - c0);
+        if (ok && rows_ok) {
+  #pragma unroll 2
+          for (int cc = ks; cc < ncol; cc += KSW) {
+            Pair<T> s;
+            s.load(S + (size_t)cc * ldn);
+            const C* v = V + (size_t)(c0 + cc) * R;
+  #pragma unroll
+            for (int r = 0; r < R; ++r) {
+              const C vr = v[r];
+              cfma(acc0[r], s.a, vr);
+              cfma(acc1[r], s.b, vr);
+            }
+          }
         }
-        const int info = rowinfo[row];
-        C* dst = Qb + ((size_t)crank * nJcap + (info & 0xffff)) * R + up * UP;
-        if (CL == 1) {
-          dst[0] = v0;
-          if (UP == 2) dst[1] = v1;
-        } else if constexpr (UP == 2) {
-          st_async2(dst, (unsigned)(info >> 16), v0, v1, &pready[buf]);
-        } else {
-          st_async(dst, (unsigned)(info >> 16), v0, &pready[buf]);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[slot]);
+      }
+      // sum the row group's column slices in shared memory, then push each
+      // row's sum to the CTA that owns the row
+      // (rows fastest: a lane's row pair is one 16-byte store per slot for
+      // float, and consecutive lanes hit consecutive banks)
+      const int RG64 = 64 * RG;
+      {
+        C* ls = LS + (size_t)ks * R * RG64 + r0;
+  #pragma unroll
+        for (int r = 0; r < R; ++r) { ls[(size_t)r * RG64] = acc0[r]; ls[(size_t)r * RG64 + 1] = acc1[r]; }
+      }
+      named_sync(3 + rg, KSW * 32);
+      {
+        constexpr int UP = (sizeof(T) == 4 && R % 2 == 0) ? 2 : 1;   // slots per store
+        constexpr int NU = R / UP;                                  // stores per row
+        const size_t lsplane = (size_t)R * RG64;
+        for (int u = ks * 32 + lane; u < 64 * NU; u += KSW * 32) {
+          const int up = u >> 6, rr = u & 63;   // consecutive lanes take consecutive rows
+          const int row = rg * 64 + rr;
+          if (row >= ny) continue;
+          const C* src = LS + (size_t)up * UP * RG64 + row;
+          C v0 = src[0], v1 = UP == 2 ? src[RG64] : czero<C>();
+          for (int q = 1; q < KSW; ++q) {
+            v0 = cadd(v0, src[q * lsplane]);
+            if (UP == 2) v1 = cadd(v1, src[q * lsplane + RG64]);
+          }
+          const int info = rowinfo[row];
+          C* dst = Qb + ((size_t)crank * nJcap + (info & 0xffff)) * R + up * UP;
+          if (CL == 1) {
+            dst[0] = v0;
+            if (UP == 2) dst[1] = v1;
+          } else if constexpr (UP == 2) {
+            st_async2(dst, (unsigned)(info >> 16), v0, v1, &pready[buf]);
+          } else {
+            st_async(dst, (unsigned)(info >> 16), v0, &pready[buf]);
+          }
         }
       }
     }
@@ -671,6 +779,7 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
         cfms(x, ek, s);
         V[e] = x;
       }
+      write_bw(e, V[e]);
     }
     named_sync(1, NSYNC);     // sync2: V holds r_{k+1} (forward) or x_k
   }
@@ -686,33 +795,35 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
 }
 
 // 16 warps (4 auxiliary + up to 3 row groups x 4 column slices) x 128 registers
-template <typename T>
+template <typename T, bool SPLIT>
 __global__ void __maxnreg__(128) k_front(FrontArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const DevItem it = a.items[blockIdx.x / a.cluster];
   const DevCell cl = a.cells[it.cell];
   const int n = it.slot_count;
   if constexpr (sizeof(T) == 4) {
-    if (n <= 1) front_body<T, 1>(a, it, cl, smem);
-    else if (n <= 2) front_body<T, 2>(a, it, cl, smem);
-    else if (n <= 4) front_body<T, 4>(a, it, cl, smem);
-    else if (n <= 8) front_body<T, 8>(a, it, cl, smem);
-    else if (n <= 12) front_body<T, 12>(a, it, cl, smem);
-    else front_body<T, 16>(a, it, cl, smem);
+    if (n <= 1) front_body<T, 1, SPLIT>(a, it, cl, smem);
+    else if (n <= 2) front_body<T, 2, SPLIT>(a, it, cl, smem);
+    else if (n <= 4) front_body<T, 4, SPLIT>(a, it, cl, smem);
+    else if (n <= 8) front_body<T, 8, SPLIT>(a, it, cl, smem);
+    else if (n <= 12) front_body<T, 12, SPLIT>(a, it, cl, smem);
+    else front_body<T, 16, SPLIT>(a, it, cl, smem);
   } else {
-    if (n <= 1) front_body<T, 1>(a, it, cl, smem);
-    else if (n <= 2) front_body<T, 2>(a, it, cl, smem);
-    else if (n <= 4) front_body<T, 4>(a, it, cl, smem);
-    else front_body<T, 8>(a, it, cl, smem);
+    if (n <= 1) front_body<T, 1, SPLIT>(a, it, cl, smem);
+    else if (n <= 2) front_body<T, 2, SPLIT>(a, it, cl, smem);
+    else if (n <= 4) front_body<T, 4, SPLIT>(a, it, cl, smem);
+    else front_body<T, 8, SPLIT>(a, it, cl, smem);
   }
 }
 
 template <typename T>
-size_t smem_need(int ldn_max, int ny_max, int nx_max, int R, int KSW, int CL, int CW, int NS) {
+size_t smem_need(int ldn_max, int ny_max, int nx_max, int R, int KSW, int CL, int CW, int NS, bool split) {
   using C = cx_t<T>;
   const int nJ = (ny_max + CL - 1) / CL + 1;
+  const size_t staging = split ? 2 * (size_t)(((nJ + 7) & ~7) + 8) * (8 * ((2 * R + 7) / 8)) * sizeof(unsigned)
+                               : (size_t)KSW * 64 * kMaxRG * R * sizeof(C);
   return kHdr + (size_t)NS * CW * ldn_max * sizeof(C) + 3 * (size_t)R * nJ * sizeof(C) + nx_max + nJ + 32 +
-         2 * (size_t)CL * R * nJ * sizeof(C) + (size_t)KSW * 64 * kMaxRG * R * sizeof(C) + 4 * (size_t)ny_max +
+         2 * (size_t)CL * R * nJ * sizeof(C) + staging + 4 * (size_t)ny_max +
          2 * (size_t)nx_max * sizeof(C) +
          (size_t)R * (sizeof(DevSlot) + sizeof(SlotCoef) + sizeof(DevGroup)) + 11 * 16;
 }
@@ -727,7 +838,13 @@ cudaError_t launch_front(const FrontArgs& a_in, int max_ny, int max_nx, cudaStre
   if (a_in.item_count <= 0) return cudaSuccess;
   FrontArgs a = a_in;
   const bool dbl = sizeof(T) == 8;
-  const int ldn = (max_ny + 3) & ~3;
+  const bool split = a.split != 0;
+  if (split && dbl) return cudaErrorInvalidValue;
+  int ldn = (max_ny + 3) & ~3;
+  if (split) {   // the split factor layout's column stride (4 mod 8)
+    ldn = max_ny;
+    while (ldn % 8 != 4) ++ldn;
+  }
   const int R = std::min(front_rpad(std::max(1, a.max_slots)), front_rmax(dbl));
   if (a.cluster < 1) a.cluster = 1;
   int dev = 0, maxopt = 0;
@@ -738,20 +855,20 @@ cudaError_t launch_front(const FrontArgs& a_in, int max_ny, int max_nx, cudaStre
   // column slices: as many as keep >= 4 columns per slice and the slices'
   // partial-sum staging (KSW x 192 x R) within 64 KB
   int KSW = kMaxKSW;
-  while (KSW > 1 && (nJmax < 4 * KSW || (size_t)KSW * 64 * kMaxRG * R * sizeof(cx_t<T>) > 65536)) --KSW;
+  while (KSW > 1 && (split || nJmax < 4 * KSW || (size_t)KSW * 64 * kMaxRG * R * sizeof(cx_t<T>) > 65536)) --KSW;
   a.ksw = KSW;
   const int cwmax = (int)std::min<size_t>(((size_t)65536 / ((size_t)ldn * sizeof(cx_t<T>))) & ~size_t(7),
                                           (size_t)((nJmax + 7) & ~7));
   int CW = std::max(8, cwmax), NS = 0;
   for (; CW >= 8; CW -= 8) {
     for (NS = 4; NS >= 2; --NS)
-      if (smem_need<T>(ldn, max_ny, max_nx, R, KSW, a.cluster, CW, NS) <= (size_t)maxopt) break;
+      if (smem_need<T>(ldn, max_ny, max_nx, R, KSW, a.cluster, CW, NS, split) <= (size_t)maxopt) break;
     if (NS >= 2) break;
   }
   if (CW < 8) return cudaErrorInvalidConfiguration;
   a.stages = NS;
   a.chunk = CW;
-  const size_t smem = smem_need<T>(ldn, max_ny, max_nx, R, KSW, a.cluster, CW, NS);
+  const size_t smem = smem_need<T>(ldn, max_ny, max_nx, R, KSW, a.cluster, CW, NS, split);
   cudaLaunchConfig_t cfg{};
   cudaLaunchAttribute attr[1];
   cfg.gridDim = dim3((unsigned)(a.item_count * a.cluster));
@@ -763,13 +880,16 @@ cudaError_t launch_front(const FrontArgs& a_in, int max_ny, int max_nx, cudaStre
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  auto kern = k_front<T>;
+  auto kern = split ? k_front<float, true> : k_front<T, false>;
   // the attribute is an upper bound: always the device maximum, so that
   // host threads launching concurrently never lower it under one another
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
   if (e != cudaSuccess) return e;
   cfg.blockDim = dim3(32 * (kAux + kMaxRG * kMaxKSW));
-  return cudaLaunchKernelEx(&cfg, kern, a);
+  if constexpr (sizeof(T) == 4) {
+    if (split) return cudaLaunchKernelEx(&cfg, k_front<float, true>, a);
+  }
+  return cudaLaunchKernelEx(&cfg, k_front<T, false>, a);
 }
 
 int front_max_clusters(bool dbl, int cluster) {
@@ -790,11 +910,12 @@ int front_max_clusters(bool dbl, int cluster) {
   int n = 0;
   cudaError_t e;
   if (dbl) {
-    cudaFuncSetAttribute(k_front<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
-    e = cudaOccupancyMaxActiveClusters(&n, k_front<double>, &cfg);
+    cudaFuncSetAttribute(k_front<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
+    e = cudaOccupancyMaxActiveClusters(&n, k_front<double, false>, &cfg);
   } else {
-    cudaFuncSetAttribute(k_front<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
-    e = cudaOccupancyMaxActiveClusters(&n, k_front<float>, &cfg);
+    cudaFuncSetAttribute(k_front<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
+    cudaFuncSetAttribute(k_front<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
+    e = cudaOccupancyMaxActiveClusters(&n, k_front<float, false>, &cfg);
   }
   if (e != cudaSuccess) {
     cudaGetLastError();

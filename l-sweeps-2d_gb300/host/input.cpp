@@ -330,14 +330,16 @@ void Input::readCheckerboardDD(UInt DDID, DD*& dd) const {
   if (!CDD.lookupValue("Solver", solverType)) need("Solver in CheckerboardDD");
   // "Eigen" (the reference's SparseLU) and "CUDA" both select the GPU cell solver
   if (solverType != "Eigen" && solverType != "CUDA") throw lsw_host_error("ERROR: unknown local solver " + solverType);
-  // extension: Precision = "fp64" (default, the reference's arithmetic) or "mixed"
+  // extension: Precision = "fp64" (default, the reference's arithmetic), "mixed" (complex64
+  // factors and sweeps) or "split" (bf16 hi + lo factor terms on the tensor cores)
   std::string prec = "fp64";
   CDD.lookupValue("Precision", prec);
-  if (prec != "fp64" && prec != "mixed") throw lsw_host_error("ERROR: Precision must be \"fp64\" or \"mixed\"");
+  if (prec != "fp64" && prec != "mixed" && prec != "split")
+    throw lsw_host_error("ERROR: Precision must be \"fp64\", \"mixed\" or \"split\"");
   LocalLinearSolverCUDA solver;
   auto* cb = new DDCheckerboard();
   try {
-    cb->setUp(&assembler, &solver, dom, {nCX, nCY}, {nX, nY}, prec == "mixed" ? LSW_PREC_C64 : LSW_PREC_C128);
+    cb->setUp(&assembler, &solver, dom, {nCX, nCY}, {nX, nY}, prec == "mixed" ? LSW_PREC_C64 : prec == "split" ? LSW_PREC_SPLIT : LSW_PREC_C128);
   } catch (...) {
     delete cb;
     throw;

@@ -13,7 +13,7 @@ LSW_OK = 0
 STATUS_NAMES = ["LSW_OK", "LSW_ERR_INVALID_ARGUMENT", "LSW_ERR_CUDA", "LSW_ERR_OUT_OF_MEMORY",
                 "LSW_ERR_NOT_SET_UP", "LSW_ERR_NOT_FACTORIZED", "LSW_ERR_SINGULAR_BLOCK",
                 "LSW_ERR_NOT_CONVERGED", "LSW_ERR_UNSUPPORTED"]
-PREC = {"c128": 0, "fp64": 0, "c64": 1, "mixed": 1}
+PREC = {"c128": 0, "fp64": 0, "c64": 1, "mixed": 1, "bf16x2": 2, "split": 2}
 GMRES_MODE = {"reference": 0, "flexible": 1}
 
 # every entry point declared in include/lsweeps.h

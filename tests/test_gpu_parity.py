@@ -3,7 +3,9 @@
 Tolerances: FP64 (complex128) factors and applies must match the oracle's
 SuperLU-based restatement to 1e-10 relative (different but exact-arithmetic-
 equivalent factorisations, so only rounding separates them); the complex64
-mixed path to 2e-4 relative on the preconditioner.  Solves: true relative
+mixed path and the bf16-split path (factor entries as bf16 hi + lo terms,
+three tensor-core products, FP32 accumulation; about 16 significant bits per
+entry) to 2e-4 relative on the preconditioner.  Solves: true relative
 residual <= 1e-6 and relative difference <= 1e-5 against the global direct
 solve; reference-mode GMRES iteration count within +-1 of the oracle."""
 from pathlib import Path
@@ -52,7 +54,7 @@ def test_apply_A_matches_oracle(f):
 
 
 @pytest.mark.parametrize("f", FIXTURES, ids=lambda p: p.stem)
-@pytest.mark.parametrize("prec,tol", [("c128", 1e-10), ("c64", 2e-4)])
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-10), ("c64", 2e-4), ("bf16x2", 2e-4)])
 def test_precond_matches_oracle(f, prec, tol):
     spec, d = _load(f)
     S = _solver(spec, d["m_grid"], prec)
@@ -60,7 +62,7 @@ def test_precond_matches_oracle(f, prec, tol):
     assert rel(y, d["Mv"]) <= tol
 
 
-@pytest.mark.parametrize("prec,tol", [("c128", 1e-10), ("c64", 2e-4)])
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-10), ("c64", 2e-4), ("bf16x2", 2e-4)])
 def test_local_solve_matches_superlu(prec, tol):
     from oracle.lsweeps_oracle import OracleProblem
     spec, med = small(N=3, m=12, p=5, medium="layered", seed=2)
@@ -90,7 +92,7 @@ def test_reference_gmres_iteration_count(f):
 
 
 @pytest.mark.parametrize("f", FIXTURES, ids=lambda p: p.stem)
-@pytest.mark.parametrize("prec", ["c128", "c64"])
+@pytest.mark.parametrize("prec", ["c128", "c64", "bf16x2"])
 def test_fgmres_solves_to_tolerance(f, prec):
     spec, d = _load(f)
     S = _solver(spec, d["m_grid"], prec)
@@ -105,7 +107,7 @@ def test_batched_rhs_equal_single():
     warps per row group depends on the slots per front)."""
     f = FIXTURES[-1]
     spec, d = _load(f)
-    for prec, tol in (("c128", 1e-13), ("c64", 1e-5)):
+    for prec, tol in (("c128", 1e-13), ("c64", 1e-5), ("bf16x2", 1e-4)):
         S = _solver(spec, d["m_grid"], prec)
         rng = np.random.default_rng(9)
         V = rng.standard_normal((3, S.n2)) + 1j * rng.standard_normal((3, S.n2))
@@ -125,7 +127,11 @@ def test_c1_precond_and_solve_match_oracle():
     S = _solver(spec, med, "c128")
     rng = np.random.default_rng(11)
     v = rng.standard_normal(S.n2) + 1j * rng.standard_normal(S.n2)
-    assert rel(S.apply_precond(_dev(v)).cpu().numpy(), P.apply_precond_global(v)) <= 1e-10
+    y_or = P.apply_precond_global(v)
+    assert rel(S.apply_precond(_dev(v)).cpu().numpy(), y_or) <= 1e-10
+    # 64-DOF cells on the tensor-core split path (eight 16-row tiles per cell)
+    Ss = _solver(spec, med, "bf16x2")
+    assert rel(Ss.apply_precond(_dev(v)).cpu().numpy(), y_or) <= 2e-4
     b = S.assemble_rhs(spec.sources)
     bo = P.global_rhs(spec.sources)
     assert rel(b.cpu().numpy(), bo) <= 1e-12

@@ -145,6 +145,19 @@ def test_driver_csv_medium_mixed_fgmres(tmp_path):
     assert d <= 1e-4, d
 
 
+def test_driver_split_precision(tmp_path):
+    omega = 2 * math.pi * 4.0
+    sources = [(0.4, 0.55)]
+    cfg = _problem_file(tmp_path, omega, 1.0, '{ Type = "Constant"; }', sources,
+                        extra_dd='Precision = "split";', extra_solver='Mode = "flexible"; Restart = 30;')
+    _run_main(cfg)
+    _, vals, _ = _read_vtk(tmp_path / "wave.vtk")
+    nd = N_G + 2 * P - 1
+    u = _python_solution(omega, np.ones((nd, nd)), sources, "c128", "flexible")
+    d = np.linalg.norm(vals - u.ravel()) / np.linalg.norm(u)
+    assert d <= 1e-4, d
+
+
 def test_driver_reports_input_errors(tmp_path):
     f = tmp_path / "bad.cfg"
     f.write_text('Problems = ( { DomainDecomposition = "CheckerboardDD"; } );')

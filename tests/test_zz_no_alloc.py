@@ -23,7 +23,7 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-@pytest.mark.parametrize("prec,tol", [("c128", 1e-10), ("c64", 2e-4)])
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-10), ("c64", 2e-4), ("bf16x2", 2e-4)])
 def test_noalloc_local_solve_matches_local_solve(prec, tol):
     from lsweeps.solver import Solver, _stream_ptr
     spec, med = small(N=3, m=12, p=5, medium="layered", seed=2)
