@@ -152,7 +152,7 @@ lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out) {
     std::vector<DevItem> items; std::vector<DevSlot> slots; std::vector<DevGroup> groups;
     try {
       FrontPlan plan;
-      plan.cluster_cap = ctx->max_cluster;
+      plan.cluster_cap = std::max(1, std::min(4, ctx->max_cluster / 2));
       plan.rmax = front_rmax(dbl);
       plan.csize = dbl ? 16 : 8;
       if (dbl) { plan.col_cost = 40.0; plan.col_slot_cost = 20.0; }
@@ -160,8 +160,8 @@ lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out) {
         // tensor-core matvec: the per-column cost hardly grows with the slots
         plan.line_overhead = 2200.0; plan.slot_cost = 0.0; plan.col_cost = 40.0; plan.col_slot_cost = 3.0;
       }
-      for (int cl = 1; cl <= 8; cl *= 2) plan.max_clusters[cl] = front_max_clusters(dbl, cl);
-      if (plan.max_clusters[1] <= 0) plan.max_clusters[1] = ctx->nsm;
+      for (int cl = 1; cl <= 4; cl *= 2) plan.max_clusters[cl] = front_max_clusters(dbl, 2 * cl);
+      if (plan.max_clusters[1] <= 0) plan.max_clusters[1] = ctx->nsm / 2;
       build_schedule(ctx->cells, ctx->N, nrhs, plan, ctx->LP, sc->fronts, items, slots, groups, ctx->n2);
     } catch (const std::exception& ex) {
       return fail(ctx, LSW_ERR_UNSUPPORTED, ex.what());
@@ -357,10 +357,11 @@ lsw_status lsw_ctx_create(lsw_ctx** out, int device) {
   c->device = device;
   int nsm = 0;
   if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) == cudaSuccess && nsm > 0) c->nsm = nsm;
-  // LSW_MAX_CLUSTER caps the CTAs per cell solve (1, 2, 4 or 8; default 8)
+  // LSW_MAX_CLUSTER caps the CTAs per cell solve (2, 4 or 8; default 8: the two
+  // halves of a cell solve always take one CTA each at least)
   if (const char* ev = std::getenv("LSW_MAX_CLUSTER")) {
     const int v = std::atoi(ev);
-    if (v >= 1 && v <= 8) c->max_cluster = v;
+    if (v >= 2 && v <= 8) c->max_cluster = v;
   }
   *out = c;
   return LSW_OK;
@@ -432,8 +433,9 @@ lsw_status lsw_problem_setup(lsw_ctx* ctx, const lsw_geom* g, const double* m_gr
   CK(ctx->d_fac.ensure((size_t)fac_off * cs), "cudaMalloc(factors)");
   CK(ctx->d_status.ensure(16), "cudaMalloc(status)");
   if (precision == LSW_PREC_SPLIT) {
-    // each cell's previous FP32 Schur-complement inverse, for the recurrence
-    CK(ctx->d_work.ensure((size_t)ctx->ncell * ctx->max_ny * (ctx->max_ny + 8) * sizeof(float2)),
+    // the previous FP32 Schur-complement inverse of each cell's two half
+    // chains, for the recurrences and the middle line
+    CK(ctx->d_work.ensure((size_t)2 * ctx->ncell * ctx->max_ny * (ctx->max_ny + 8) * sizeof(float2)),
        "cudaMalloc(factor work)");
   }
   CK(cudaMemcpy(ctx->d_cells.p, ctx->cells.data(), ctx->cells.size() * sizeof(DevCell), cudaMemcpyHostToDevice), "H2D cells");
@@ -472,7 +474,7 @@ lsw_status lsw_factorize(lsw_ctx* ctx, void* stream) {
   CK(cudaSetDevice(ctx->device), "cudaSetDevice");
   cudaStream_t st = S(stream);
   CK(cudaMemsetAsync(ctx->d_status.p, 0, 16, st), "memset status");
-  ctx->launches += 1;
+  ctx->launches += 2;   // half chains, middle lines
   const double w2 = ctx->omega * ctx->omega;
   cudaError_t e = ctx->prec != LSW_PREC_C128
                       ? launch_factorize<float>(ctx->d_cells.as<DevCell>(), ctx->ncell, ctx->d_prof.as<double2>(),
@@ -612,7 +614,7 @@ lsw_status lsw_local_solve(lsw_ctx* ctx, int cell, const void* b, void* x, int n
     it.cell = cell; it.slot_begin = (int)slots.size(); it.group_begin = 0; it.group_count = 0;
     it.slot_count = std::min(rmax, nrhs - r0);
     it.scratch_off = scr;
-    scr += (long long)cl.nx * front_rpad(it.slot_count) * cl.ny;
+    scr += (long long)(cl.nx + 1) * front_rpad(it.slot_count) * cl.ny;
     for (int r = r0; r < r0 + it.slot_count; ++r) {
       DevSlot s{};
       s.kind = SK_CELLVEC; s.rhs = r;
@@ -644,7 +646,7 @@ lsw_status lsw_local_solve(lsw_ctx* ctx, int cell, const void* b, void* x, int n
   a.max_slots = std::min(rmax, nrhs);
   a.err = ctx->d_status.as<int>() + 1;
   a.split = ctx->prec == LSW_PREC_SPLIT ? 1 : 0;
-  a.cluster = std::min(ctx->max_cluster, front_cluster(a.item_count, ctx->nsm));
+  a.cluster = front_cluster(a.item_count, ctx->nsm, ctx->max_cluster);
   cudaError_t e = dbl ? launch_front<double>(a, ctx->max_ny, ctx->max_nx, st) : launch_front<float>(a, ctx->max_ny, ctx->max_nx, st);
   CK(e, "local solve kernel");
   ctx->launches += 1;
@@ -1018,7 +1020,7 @@ lsw_status lsw_local_solve_noalloc(lsw_ctx* ctx, int cell, const void* b, void* 
   const int rmax = front_rmax(dbl);
   const DevCell& cl = ctx->cells[cell];
   const int n_items = (nrhs + rmax - 1) / rmax;
-  const long long per_item = (long long)cl.nx * front_rpad(std::min(rmax, nrhs)) * cl.ny;
+  const long long per_item = (long long)(cl.nx + 1) * front_rpad(std::min(rmax, nrhs)) * cl.ny;
   const size_t desc_bytes = ((size_t)n_items * sizeof(DevItem) + (size_t)nrhs * sizeof(DevSlot) + 255) & ~size_t(255);
   const size_t need = desc_bytes + (size_t)n_items * per_item * csize(ctx->prec);
   if (need > kNoAllocScratchBytes) {
@@ -1065,7 +1067,7 @@ lsw_status lsw_local_solve_noalloc(lsw_ctx* ctx, int cell, const void* b, void* 
   a.max_slots = std::min(rmax, nrhs);
   a.err = ctx->d_status.as<int>() + 1;
   a.split = ctx->prec == LSW_PREC_SPLIT ? 1 : 0;
-  a.cluster = std::min(ctx->max_cluster, front_cluster(a.item_count, ctx->nsm));
+  a.cluster = front_cluster(a.item_count, ctx->nsm, ctx->max_cluster);
   cudaError_t e = dbl ? launch_front<double>(a, ctx->max_ny, ctx->max_nx, st) : launch_front<float>(a, ctx->max_ny, ctx->max_nx, st);
   CK(e, "local solve kernel");
   ctx->launches += 2;

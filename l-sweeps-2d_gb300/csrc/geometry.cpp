@@ -321,13 +321,16 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
       }
       if (n_items == 0) continue;
       const int R = front_rpad(maxs);
+      // an item is a cluster of two halves of cl CTAs, each running
+      // 2 nf + 1 lines of the twisted solve (nf forward lines of the longer half)
+      const int nf = nx_max - 1 - (nx_max - 1) / 2;
       for (int cl = 1; cl <= plan.cluster_cap; cl *= 2) {
         const int mc = std::max(1, plan.max_clusters[cl]);
         if (plan.max_clusters[cl] <= 0 && cl > 1) continue;
         const long long waves = (n_items + mc - 1) / mc;
         const double line = plan.line_overhead + plan.slot_cost * R +
                             (plan.col_cost + plan.col_slot_cost * R) * ((ny_max + cl - 1) / cl);
-        double t = (double)waves * (2.0 * nx_max - 1.0) * line;
+        double t = (double)waves * (2.0 * nf + 1.0) * line;
         t = std::max(t, fac_elems * plan.csize / plan.bytes_per_cycle);
         // ties go to fewer items (less factor traffic), then to larger clusters
         if (t < best_t * 0.98 || (t <= best_t * 1.02 && n_items < best_items)) {
@@ -357,7 +360,7 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
         }
         it.slot_count = count;
         it.scratch_off = F.scratch_elems;
-        F.scratch_elems += (long long)cl.nx * front_rpad(it.slot_count) * cl.ny;
+        F.scratch_elems += (long long)(cl.nx + 1) * front_rpad(it.slot_count) * cl.ny;
         F.max_slots = std::max(F.max_slots, it.slot_count);
         items.push_back(it);
         F.item_count++;

@@ -103,8 +103,9 @@ struct Front {
 //   line_overhead + slot_cost R + (col_cost + col_slot_cost R) x columns per CTA,
 // with a bandwidth floor (factor bytes / bytes_per_cycle).
 struct FrontPlan {
+  // indexed by the CTAs per half (1, 2, 4): resident clusters of twice that many CTAs
   int max_clusters[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  int cluster_cap = 8;
+  int cluster_cap = 4;       // CTAs per half
   int rmax = 16;
   int csize = 8;             // bytes per complex value of the factors
   double line_overhead = 1800.0;
@@ -163,10 +164,11 @@ struct FrontArgs {
   int ksw;                // consumer column slices (set by the launcher)
   int split;              // factors hold bf16 hi/lo terms; the matvec runs on mma.sync
 };
-// CTAs per item for a front of `items` cell solves on `nsm` SMs
-inline int front_cluster(int items, int nsm) {
-  int cl = 8;
-  while (cl > 1 && items * cl > nsm) cl >>= 1;
+// CTAs per half of an item (the item's cluster holds two halves) for a
+// front of `items` cell solves on `nsm` SMs, with at most `max_cta` CTAs per item
+inline int front_cluster(int items, int nsm, int max_cta) {
+  int cl = 4;
+  while (cl > 1 && (items * 2 * cl > nsm || 2 * cl > max_cta)) cl >>= 1;
   return cl;
 }
 

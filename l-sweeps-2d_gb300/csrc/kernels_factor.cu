@@ -4,10 +4,17 @@
 //
 // The cell matrix is block tridiagonal over its nx x-lines, with tridiagonal
 // diagonal blocks D_k (5-point stencil along y) and couplings w_k I / e_k I to
-// the neighbouring lines.  Block LU gives the Schur complements
-//   S_0 = D_0,   S_k = D_k - w_k e_{k-1} S_{k-1}^{-1},
-// and the factor kept for the solves is Sinv_k = S_k^{-1} for every line,
-// stored column-major (element (i, j) at j*ldn + i).
+// the neighbouring lines.  It is factorised from both ends towards the middle
+// line m = (nx - 1) / 2 (a twisted block LU, "burn at both ends"): the
+// Schur complements
+//   top     S_0 = D_0,            S_k = D_k - w_k e_{k-1} S_{k-1}^{-1}   (k < m)
+//   bottom  T_{nx-1} = D_{nx-1},  T_k = D_k - e_k w_{k+1} T_{k+1}^{-1}   (k > m)
+//   middle  Z_m = D_m - w_m e_{m-1} S_{m-1}^{-1} - e_m w_{m+1} T_{m+1}^{-1}
+// are inverted, and line k of the factor holds S_k^{-1}, Z_m^{-1} or
+// T_k^{-1}, column-major (element (i, j) at j*ldn + i).  A solve then runs two
+// independent chains of about nx / 2 lines each way instead of one chain of
+// 2 nx - 1 lines (kernels_sweep.cu).  The two half chains of every cell run in
+// one launch (a cluster per cell and half), the middle lines in a second.
 //
 // Each S_k is inverted in place by Gauss-Jordan elimination with partial
 // pivoting on unpivoted rows (implicit row exchange, pivot order recorded;
@@ -132,7 +139,8 @@ template <typename T>
 __global__ void __launch_bounds__(kFT, 1)
 k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
             const double* __restrict__ mgrid, int n_dof, double omega2, cx_t<T>* __restrict__ fac,
-            cx_t<T>* __restrict__ prev, long long prev_stride, int split, int G, int nmax, int ldw, int* status) {
+            cx_t<T>* __restrict__ prev, long long prev_stride, int split, int middle, int G, int nmax, int ldw,
+            int* status) {
   using C = cx_t<T>;
   constexpr int CJ = FacCfg<T>::CJ;
   constexpr int kB = FacCfg<T>::B;
@@ -143,8 +151,14 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
     if (tid == 0) atomicOr(status, 4);   // the launch did not form the expected clusters
     return;
   }
-  const DevCell cl = cells[blockIdx.x / G];
+  // middle == 0: cluster (cell, half) runs the top (half 0) or bottom (half 1)
+  // chain; middle == 1: cluster `cell` forms and inverts Z_m
+  const int cidx = middle ? (int)(blockIdx.x / G) : (int)(blockIdx.x / (2 * G));
+  const int half = middle ? 0 : (int)((blockIdx.x / G) & 1);
+  const DevCell cl = cells[cidx];
   const int n = cl.ny, nx = cl.nx, ldn = cl.ldn;
+  const int mid = (nx - 1) / 2;
+  const int nsteps = middle ? 1 : (half == 0 ? mid : nx - 1 - mid);
   const int c0 = (int)g * n / G, c1 = ((int)g + 1) * n / G, nc = c1 - c0;
 
   // ---- shared layout (identical in every CTA of the cluster) ----
@@ -167,7 +181,10 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
   const double2* px = prof + cl.prof_off;  // lo_x, hi_x, dg_x, lo_y, hi_y, dg_y
   const double2* py = px + 3 * nx;
   C* Fac = fac + cl.fac_off;
-  C* Prev = prev ? prev + (long long)(blockIdx.x / G) * prev_stride : nullptr;   // split: Sinv_{k-1} in FP32
+  // split: the last inverse of each half chain in FP32, [cell][half]
+  C* Prev0 = prev ? prev + (long long)(2 * cidx) * prev_stride : nullptr;
+  C* Prev1 = prev ? Prev0 + prev_stride : nullptr;
+  C* Prev = half ? Prev1 : Prev0;
   const C z = czero<C>();
 
   if (tid == 0) {
@@ -204,17 +221,32 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
     return *abort_flag == 0;
   };
 
-  for (int k = 0; k < nx; ++k) {
-    // ---- Schur complement S_k, my columns, into W (row-major) ----
+  for (int step = 0; step < nsteps; ++step) {
+    const int k = middle ? mid : (half == 0 ? step : nx - 1 - step);
+    // ---- Schur complement of line k, my columns, into W (row-major) ----
+    // one or two coupled neighbour inverses: the previous line of the chain,
+    // or both neighbours of the middle line
     const C dgx = to_c(px[2 * nx + k], z);
-    C coup = z;
-    if (k > 0) coup = cmul(to_c(px[k], z), to_c(px[nx + k - 1], z));   // w_k e_{k-1}
-    const C* Fp = split ? Prev : Fac + (size_t)(k - 1) * n * ldn;
+    C coupa = z, coupb = z;
+    const C* Fa = nullptr;
+    const C* Fb = nullptr;
+    if (middle) {
+      coupa = cmul(to_c(px[k], z), to_c(px[nx + k - 1], z));   // w_m e_{m-1}
+      coupb = cmul(to_c(px[nx + k], z), to_c(px[k + 1], z));   // e_m w_{m+1}
+      Fa = split ? Prev0 : Fac + (size_t)(k - 1) * n * ldn;
+      Fb = split ? Prev1 : Fac + (size_t)(k + 1) * n * ldn;
+    } else if (step > 0) {
+      const int kp = half == 0 ? k - 1 : k + 1;
+      coupa = half == 0 ? cmul(to_c(px[k], z), to_c(px[nx + k - 1], z))    // w_k e_{k-1}
+                        : cmul(to_c(px[nx + k], z), to_c(px[k + 1], z));   // e_k w_{k+1}
+      Fa = split ? Prev : Fac + (size_t)kp * n * ldn;
+    }
     const double* mrow = mgrid + (long long)(cl.lox + k) * n_dof + cl.loy;
     for (int e = tid; e < n * nc; e += kFT) {
       const int cc = e / n, i = e - cc * n, j = c0 + cc;
       C v = z;
-      if (k > 0) v = cneg(cmul(coup, Fp[(size_t)j * ldn + i]));
+      if (Fa) v = cneg(cmul(coupa, Fa[(size_t)j * ldn + i]));
+      if (Fb) cfms(v, coupb, Fb[(size_t)j * ldn + i]);
       if (j == i) {
         C d = cadd(dgx, to_c(py[2 * n + i], z));
         d.x -= (T)(omega2 * mrow[i]);
@@ -421,7 +453,7 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
       const C v = (i < n) ? W[(size_t)piv[i] * ldw + cc] : z;
       if constexpr (sizeof(T) == 4) {
         if (split) {
-          Prev[(size_t)j * ldn + i] = v;
+          if (!middle) Prev[(size_t)j * ldn + i] = v;
           reinterpret_cast<uint2*>(Fk)[(size_t)j * ldn + i] = split_entry(v);
           continue;
         }
@@ -483,9 +515,12 @@ cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* pro
   // host threads launching concurrently never lower it under one another
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
   if (e != cudaSuccess) return e;
+  if (split && (sizeof(T) != 4 || prev == nullptr)) return cudaErrorInvalidValue;
+  // split: the last FP32 inverse of each half chain, max_ny x ldn_max complex
+  // per (cell, half) (ldn_max <= max_ny + 7)
+  const long long prev_stride = (long long)max_ny * (max_ny + 8);
   cudaLaunchConfig_t cfg{};
   cudaLaunchAttribute attr[1];
-  cfg.gridDim = dim3((unsigned)(ncell * G));
   cfg.blockDim = dim3(kFT);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
@@ -495,12 +530,15 @@ cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* pro
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (split && (sizeof(T) != 4 || prev == nullptr)) return cudaErrorInvalidValue;
-  // previous-block buffer: max_ny x ldn_max complex per cell (ldn_max <= max_ny + 7)
-  const long long prev_stride = (long long)max_ny * (max_ny + 8);
-  return cudaLaunchKernelEx(&cfg, kern, cells, prof, mgrid, n_dof, omega2, reinterpret_cast<cx_t<T>*>(fac),
-                            reinterpret_cast<cx_t<T>*>(split ? prev : nullptr), prev_stride, split ? 1 : 0, G,
-                            max_ny, ldw, status);
+  // both half chains of every cell, then every middle line (stream order)
+  for (int middle = 0; middle < 2; ++middle) {
+    cfg.gridDim = dim3((unsigned)(ncell * G * (middle ? 1 : 2)));
+    e = cudaLaunchKernelEx(&cfg, kern, cells, prof, mgrid, n_dof, omega2, reinterpret_cast<cx_t<T>*>(fac),
+                           reinterpret_cast<cx_t<T>*>(split ? prev : nullptr), prev_stride, split ? 1 : 0, middle,
+                           G, max_ny, ldw, status);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 

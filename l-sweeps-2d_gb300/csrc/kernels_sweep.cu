@@ -3,21 +3,32 @@
 //
 // A cell matrix is block tridiagonal over its x-lines (DOF order i*ny + j,
 // AssemblerHelmholtz2DFD.cpp:166-177); the couplings between lines are scalar
-// multiples of the identity (the PML profile is separable), so with the stored
-// Schur-complement inverses Sinv_k (kernels_factor.cu) a solve is
-//   forward   y_k = Sinv_k (b_k - w_k y_{k-1})
-//   backward  x_k = y_k - e_k Sinv_k x_{k+1}
-// (w_k, e_k = couplings of line k to k-1 / k+1).  One cell solve ("item")
-// carries R right-hand sides ("slots") that share every factor block read.
+// multiples of the identity (the PML profile is separable).  The factor
+// (kernels_factor.cu) is a twisted block LU about the middle line
+// m = (nx - 1) / 2, so a solve is two independent chains that meet there:
+//   top     y_k = S_k^{-1} (b_k - w_k y_{k-1})           k = 0 .. m-1
+//   bottom  z_k = T_k^{-1} (b_k - e_k z_{k+1})           k = nx-1 .. m+1
+//   middle  x_m = Z_m^{-1} (b_m - w_m y_{m-1} - e_m z_{m+1})
+//   top     x_k = y_k - e_k S_k^{-1} x_{k+1}             k = m-1 .. 0
+//   bottom  x_k = z_k - w_k T_k^{-1} x_{k-1}             k = m+1 .. nx-1
+// (w_k, e_k = couplings of line k to k-1 / k+1): about nx + 1 dependent
+// matvecs per half instead of 2 nx - 1 for a one-ended block LU.  One cell
+// solve ("item") carries R right-hand sides ("slots") that share every factor
+// block read.
 //
-// Work split.  An item runs on a thread-block cluster of CL CTAs; CTA c owns
-// the column range J_c of every block (contiguous in the column-major factor)
-// and the same range of every line vector.  Per line it forms the partial
-// products of all rows with its columns and pushes the partial sums of each
-// row to the CTA that owns that row (st.async into the owner's shared memory,
-// completing the transaction count of the owner's per-line mbarrier; no
-// fences or remote arrives on the per-line path), so every SM streams 1/CL of
-// the factor and reads only local shared memory when it finishes a line.
+// Work split.  An item runs on a thread-block cluster of 2 CL CTAs: CTAs
+// 0..CL-1 run the top chain and CL..2CL-1 the bottom chain.  Within a half,
+// CTA c owns the column range J_c of every block (contiguous in the
+// column-major factor) and the same range of every line vector.  Per line it
+// forms the partial products of all rows with its columns and pushes the
+// partial sums of each row to the CTA of its half that owns that row
+// (st.async into the owner's shared memory, completing the transaction count
+// of the owner's per-line mbarrier; no fences or remote arrives on the
+// per-line path), so every SM streams 1/CL of its half's blocks and reads only
+// local shared memory when it finishes a line.  Before the middle line, CTA c
+// of each half sends its y_{m-1} / z_{m+1} columns to CTA c of the other half
+// (same column range), and both halves run the middle line on identical
+// inputs, so both hold the same x_m.
 //
 // Roles inside a CTA: warp 0 is the producer that streams the CTA's column
 // chunks (CW columns, contiguous, up to ~64 KB: one bulk copy costs ~700
@@ -32,7 +43,8 @@
 // no cross-lane reduction.  Line vectors and partial sums are stored
 // [column][slot] so that slot offsets are compile-time constants.  The
 // outputs (owned DOFs, trace lines, cell vectors) are written once per item
-// from the scratch by every non-producer thread after the backward pass.
+// from the scratch by every non-producer thread after the backward pass, each
+// half writing its own lines.
 // Every wait is bounded: after ~2 s of clock cycles a wait raises the CTA's
 // abort flag and *a.err, and all later waits return at once so every thread
 // still reaches every barrier.
@@ -279,18 +291,34 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   using C = cx_t<T>;
   const int CW = a.chunk;              // columns per chunk, multiple of 8
   const int KSW = a.ksw;               // column slices: consumer warps per row group
-  static_assert((2 * kNSMax + 3) * 8 + 4 <= kHdr, "barrier header");
+  static_assert((2 * kNSMax + 4) * 8 + 4 <= kHdr, "barrier header");
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nx = cl.nx, ny = cl.ny, ldn = cl.ldn;
-  const int CL = a.cluster;
+  const int CL = a.cluster;              // CTAs per half
+  const int CLT = 2 * CL;                // CTAs per item
   const int NS = a.stages;
-  const unsigned crank = CL > 1 ? cluster_rank() : 0u;
-  if (CL > 1 && (cluster_size() != (unsigned)CL || crank != blockIdx.x % (unsigned)CL)) {
+  const unsigned crk = cluster_rank();
+  if (cluster_size() != (unsigned)CLT || crk != blockIdx.x % (unsigned)CLT) {
     // the launch did not form the clusters this kernel was configured for
     // (uniform over the CTA: every thread leaves before any barrier)
     if (threadIdx.x == 0) atomicOr(a.err, 4);
     return;
   }
+  const int half = (int)crk / CL;        // 0: top chain, 1: bottom chain
+  const unsigned crank = crk % (unsigned)CL;          // rank within the half
+  const unsigned rbase = (unsigned)(half * CL);       // cluster rank of the half's CTA 0
+  const unsigned partner = (unsigned)((1 - half) * CL) + crank;
+  const int mid = (nx - 1) / 2;
+  const int nf = half == 0 ? mid : nx - 1 - mid;      // forward lines of my half (>= 2: nx >= 5)
+  // line li of my half: forward li < nf, the middle line li == nf, backward after
+  auto line_k = [&](int li) {
+    const int i = li < nf ? li : 2 * nf - li;
+    if (li == nf) return mid;
+    return half == 0 ? i : nx - 1 - i;
+  };
+  // scratch row of line k; the bottom half keeps its copy of b_m in row nx
+  auto srow = [&](int k) { return (half == 1 && k == mid) ? nx : k; };
+  const int klo = half == 0 ? 0 : mid + 1, khi = half == 0 ? mid : nx - 1;   // lines whose outputs I write
   const int jb = (int)crank * ny / CL, je = ((int)crank + 1) * ny / CL;
   const int nJ = je - jb;               // my columns / rows of every line
   const int RG = (ny + 63) >> 6;        // row groups of 64 rows
@@ -302,14 +330,15 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   const int NSYNC = NCT + 96;           // consumers + 2 helper warps + writer warp
   const int nch = (nJ + CW - 1) / CW;   // chunks per line
   const int nslot = it.slot_count;
-  const int nline = 2 * nx - 1;         // forward 0..nx-1, backward nx-2..0
+  const int nline = 2 * nf + 1;         // forward, middle, backward
 
   // ---- shared layout ----
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);
   uint64_t* empty = full + kNSMax;
   uint64_t* pready = empty + kNSMax;    // [2]: every CTA's partial sums of my rows have landed (CL > 1)
   uint64_t* exitb = pready + 2;         // cluster-wide "done with remote shared memory"
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(exitb + 1);
+  uint64_t* xch = exitb + 1;            // the other half's last forward vector has landed in P
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(xch + 1);
   auto al16 = [](unsigned char* q) {
     return reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(q) + 15) & ~uintptr_t(15));
   };
@@ -327,6 +356,8 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   C* H = reinterpret_cast<C*>(p);       // [nJ][R]  helper: next right-hand side or stored y_k
   p = al16(p + (size_t)R * nJcap * sizeof(C));
   C* Y = reinterpret_cast<C*>(p);       // [nJ][R]  y_k staged for the writer (forward)
+  p = al16(p + (size_t)R * nJcap * sizeof(C));
+  C* P = reinterpret_cast<C*>(p);       // [nJ][R]  the other half's y_{m-1} / z_{m+1}, my columns
   p = al16(p + (size_t)R * nJcap * sizeof(C));
   unsigned char* colf = p;              // [nJ] bit 0: grid line; bits 1, 2: owned in y (non-shifted, shifted)
   p = al16(p + nJcap);
@@ -387,7 +418,7 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   if (tid < it.group_count) gr[tid] = a.groups[it.group_begin + tid];
   for (int row = tid; row < ny; row += blockDim.x) {
     const int o = owner_of(row, ny, CL);
-    rowinfo[row] = (o << 16) | (row - o * ny / CL);
+    rowinfo[row] = (((int)rbase + o) << 16) | (row - o * ny / CL);
   }
   for (int k = tid; k < nx; k += blockDim.x)
     linef[k] = (unsigned char)((is_line(cl.lox + k - a.p + 1, a.m, a.N) ? 1 : 0) |
@@ -417,25 +448,28 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
     // land by st.async and complete the transaction count
     mbar_init(&pready[0], 1);
     mbar_init(&pready[1], 1);
-    mbar_init(&exitb[0], CL * NCW);
+    mbar_init(&exitb[0], CLT * NCW);
+    // one phase: the partner CTA's forward vector (its columns = mine)
+    mbar_init(xch, 1);
+    mbar_expect_tx(xch, (unsigned)(nJ * R * sizeof(C)));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  if (CL > 1) {
-    // every CTA's barriers are initialised before anyone arrives remotely
-    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-  }
+  // every CTA's barriers are initialised before anyone arrives remotely
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 
-  // Right-hand sides of every line of the item into its scratch rows (row k
-  // then holds b_k until the forward pass replaces it with y_k, and the
-  // backward pass with x_k), computed once per item by every non-producer
-  // thread so that the per-line helpers only copy a contiguous row.
+  // Right-hand sides of every line of my half and of the middle line into
+  // the item's scratch rows (row k then holds b_k until the forward pass
+  // replaces it with y_k / z_k, and the backward pass with x_k), computed once
+  // per item by every non-producer thread so that the per-line helpers only
+  // copy a contiguous row.
   // A volume slot of shift (sx, sy) takes the owned DOFs whose x- and y-line
   // status matches the shift (the windows of getSeparatedRHS).
   auto prologue = [&](int et) {
     const int per_line = nJ * R;
-    for (int e = et; e < nx * per_line; e += NSYNC) {
-      const int k = e / per_line, rem = e - k * per_line;
+    for (int e = et; e < (nf + 1) * per_line; e += NSYNC) {
+      const int lr = e / per_line, rem = e - lr * per_line;
+      const int k = half == 0 ? lr : (lr < nf ? mid + 1 + lr : mid);
       const int jj = rem / R, r = rem - jj * R, j = jb + jj;
       const DevSlot& sr = sl[r];
       C v = czero<C>();
@@ -447,7 +481,7 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
       } else if (sr.kind != SK_NONE) {
         v = rhs_elem<T>(a, cl, sr, cf[r], tr, k, j);
       }
-      scr[((size_t)k * ny + jb) * R + rem] = v;
+      scr[((size_t)srow(k) * ny + jb) * R + rem] = v;
     }
   };
 
@@ -463,7 +497,8 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
       const DevGroup G = gr[g];
       if (G.out_off < 0) continue;
       const int sx = G.shift & 1, sy = (G.shift >> 1) & 1;
-      const int k0 = sx ? cl.ownx[1][0] : cl.ownx[0][0], k1 = sx ? cl.ownx[1][1] : cl.ownx[0][1];
+      const int k0 = max(sx ? cl.ownx[1][0] : cl.ownx[0][0], klo);
+      const int k1 = min(sx ? cl.ownx[1][1] : cl.ownx[0][1], khi);
       const int j0 = max(sy ? cl.owny[1][0] : cl.owny[0][0], jb);
       const int j1 = min(sy ? cl.owny[1][1] : cl.owny[0][1], je - 1);
       const int w = j1 - j0 + 1, hg = k1 - k0 + 1;
@@ -479,8 +514,8 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
       const DevSlot& sr = sl[r];
       if (sr.kind == SK_NONE) continue;
       if (sr.kind == SK_CELLVEC) {
-        for (int e = et; e < nx * nJ; e += NSYNC) {
-          const int k = e / nJ, j = jb + (e - (e / nJ) * nJ);
+        for (int e = et; e < (khi - klo + 1) * nJ; e += NSYNC) {
+          const int k = klo + e / nJ, j = jb + (e - (e / nJ) * nJ);
           a.x_out[(long long)sr.rhs * a.out_stride + (long long)k * ny + j] = to_c(xat(k, r, j), make_double2(0, 0));
         }
         continue;
@@ -496,13 +531,13 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
       };
       for (int l = 0; l < sr.n_lr; ++l) {
         const int k = sr.lr_line[l];
-        if (k < 0 || k >= nx) continue;
+        if (k < klo || k > khi) continue;
         for (int jj = et; jj < nJ; jj += NSYNC) red_add(trw + sr.lr_out[l] + jb + jj, tval(k, jb + jj));
       }
       for (int l = 0; l < sr.n_ud; ++l) {
         const int j = sr.ud_line[l];
         if (j < jb || j >= je) continue;
-        for (int k = et; k < nx; k += NSYNC) red_add(trw + sr.ud_out[l] + k, tval(k, j));
+        for (int k = klo + et; k <= khi; k += NSYNC) red_add(trw + sr.ud_out[l] + k, tval(k, j));
       }
     }
   };
@@ -512,8 +547,7 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
     if (lane < 2) {
       long long idx = 0;
       for (int li = 0; li < nline; ++li) {
-        const int k = li < nx ? li : 2 * nx - 2 - li;
-        const C* blk = fac + (size_t)k * ny * ldn;
+        const C* blk = fac + (size_t)line_k(li) * ny * ldn;
         for (int c = 0; c < nch; ++c, ++idx) {
           if ((idx & 1) != lane) continue;   // lanes 0 and 1 issue alternate chunks
           const int slot = (int)(idx % NS);
@@ -550,16 +584,14 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
     };
     prologue(NCT + ht);
     named_sync(1, NSYNC);     // every b_k is in scratch
-    fetch(0);
-    named_sync(1, NSYNC);     // S0: H = b_0
+    fetch(srow(line_k(0)));
+    named_sync(1, NSYNC);     // S0: H = b of my first line
     named_sync(1, NSYNC);     // S0b: consumers copied it into V
     for (int li = 0; li < nline; ++li) {
-      const bool fwd = li < nx;
-      const int k = fwd ? li : 2 * nx - 2 - li;
-      if (fwd) {
-        if (k + 1 < nx) fetch(k + 1);   // b_{k+1}
-      } else {
-        fetch(k);                       // y_k
+      if (li < nf) {
+        fetch(srow(line_k(li + 1)));    // b of the next line (the middle line's after the last)
+      } else if (li > nf) {
+        fetch(line_k(li));              // y_k / z_k
       }
       named_sync(1, NSYNC);   // sync1
       named_sync(1, NSYNC);   // sync2
@@ -576,12 +608,12 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
     named_sync(1, NSYNC);     // S0
     named_sync(1, NSYNC);     // S0b
     for (int li = 0; li < nline; ++li) {
-      const bool fwd = li < nx;
-      const int k = fwd ? li : 2 * nx - 2 - li;
+      const int k = line_k(li);
       named_sync(1, NSYNC);   // sync1
-      named_sync(1, NSYNC);   // sync2: Y (forward y_k) or V (backward x_k) is complete
-      // forward y_k (on the last line equal to x_k), backward x_k over it
-      const C* src = fwd ? Y : V;
+      named_sync(1, NSYNC);   // sync2: Y (forward y_k / z_k, middle x_m) or V (backward x_k) is complete
+      // forward y_k / z_k, then backward x_k over it; x_m by the top half only
+      if (li == nf && half == 1) continue;
+      const C* src = li <= nf ? Y : V;
       C* dst = scr + ((size_t)k * ny + jb) * R;
       for (int e = lane; e < R * nJ; e += 32) dst[e] = src[e];
     }
@@ -627,8 +659,7 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   if (CL > 1 && ct == 0) mbar_expect_tx(&pready[0], line_bytes);
   long long idx = 0;
   for (int li = 0; li < nline; ++li) {
-    const bool fwd = li < nx;
-    const int k = fwd ? li : 2 * nx - 2 - li;
+    const int k = line_k(li);
     const int buf = li & 1;
     // arm the next line's barrier: its buffer was last read before the
     // previous sync2 (peers' bytes may land before this; the phase cannot
@@ -758,38 +789,74 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
     named_sync(1, NSYNC);     // sync1: partials (cluster-wide) and H complete
 
     // ---- finish the line for my rows, element-wise ----
-    const C wk = (fwd && k + 1 < nx) ? wsh[k + 1] : czero<C>();
-    const C ek = esh[k];
+    // couplings toward the previous / next line of my chain: (w, e) for the
+    // top half, (e, w) for the bottom half
     const int nplane = CL;
-    for (int e = ct; e < R * nJ; e += NCT) {
-      C s = czero<C>();
-      const C* q = Qb + e;
-      for (int pl = 0; pl < nplane; ++pl, q += qplane) s = cadd(s, *q);
-      if (fwd) {
+    if (li < nf) {
+      // forward: y_k / z_k, then the next line's input
+      const bool last = li + 1 == nf;
+      const int kn = last ? mid : line_k(li + 1);
+      const C cp = half == 0 ? wsh[kn] : esh[kn];
+      for (int e = ct; e < R * nJ; e += NCT) {
+        C s = czero<C>();
+        const C* q = Qb + e;
+        for (int pl = 0; pl < nplane; ++pl, q += qplane) s = cadd(s, *q);
         Y[e] = s;
-        if (k + 1 < nx) {
+        if (!last) {
           C b = H[e];
-          cfms(b, wk, s);
+          cfms(b, cp, s);
           V[e] = b;
+          write_bw(e, b);
         } else {
-          V[e] = s;   // x_{K-1} = y_{K-1}
+          st_async(P + e, partner, s, xch);   // to the other half's CTA with my columns
         }
-      } else {
-        C x = H[e];
-        cfms(x, ek, s);
-        V[e] = x;
       }
-      write_bw(e, V[e]);
+      if (last) {
+        // middle input b_m - w_m y_{m-1} - e_m z_{m+1}, formed in the same
+        // order in both halves so that both compute the same x_m
+        mbar_wait<true>(xch, 0u, a.err, abort_flag);
+        const C wm = wsh[mid], em = esh[mid];
+        for (int e = ct; e < R * nJ; e += NCT) {
+          const C own = Y[e], oth = P[e];
+          C b = H[e];
+          cfms(b, wm, half == 0 ? own : oth);
+          cfms(b, em, half == 0 ? oth : own);
+          V[e] = b;
+          write_bw(e, b);
+        }
+      }
+    } else if (li == nf) {
+      // middle: x_m, the first backward input of both halves
+      for (int e = ct; e < R * nJ; e += NCT) {
+        C s = czero<C>();
+        const C* q = Qb + e;
+        for (int pl = 0; pl < nplane; ++pl, q += qplane) s = cadd(s, *q);
+        Y[e] = s;
+        V[e] = s;
+        write_bw(e, s);
+      }
+    } else {
+      // backward: x_k = y_k - e_k (S_k^{-1} x_{k+1}) or z_k - w_k (T_k^{-1} x_{k-1})
+      const C cn = half == 0 ? esh[k] : wsh[k];
+      for (int e = ct; e < R * nJ; e += NCT) {
+        C s = czero<C>();
+        const C* q = Qb + e;
+        for (int pl = 0; pl < nplane; ++pl, q += qplane) s = cadd(s, *q);
+        C x = H[e];
+        cfms(x, cn, s);
+        V[e] = x;
+        write_bw(e, x);
+      }
     }
-    named_sync(1, NSYNC);     // sync2: V holds r_{k+1} (forward) or x_k
+    named_sync(1, NSYNC);     // sync2: V holds the next line's input
   }
   named_sync(1, NSYNC);       // every x_k is stored
   epilogue(ct);
 
-  if (CL > 1) {
-    // nobody leaves while a peer may still read its partial sums
+  {
+    // nobody leaves while a peer may still write into its shared memory
     __syncwarp();
-    if (lane < CL) mbar_arrive_remote(&exitb[0], (unsigned)lane);
+    if (lane < CLT) mbar_arrive_remote(&exitb[0], (unsigned)lane);
     mbar_wait<true>(&exitb[0], 0u, a.err, abort_flag);
   }
 }
@@ -798,7 +865,7 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
 template <typename T, bool SPLIT>
 __global__ void __maxnreg__(128) k_front(FrontArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
-  const DevItem it = a.items[blockIdx.x / a.cluster];
+  const DevItem it = a.items[blockIdx.x / (2 * a.cluster)];
   const DevCell cl = a.cells[it.cell];
   const int n = it.slot_count;
   if constexpr (sizeof(T) == 4) {
@@ -822,10 +889,10 @@ size_t smem_need(int ldn_max, int ny_max, int nx_max, int R, int KSW, int CL, in
   const int nJ = (ny_max + CL - 1) / CL + 1;
   const size_t staging = split ? 2 * (size_t)(((nJ + 7) & ~7) + 8) * (8 * ((2 * R + 7) / 8)) * sizeof(unsigned)
                                : (size_t)KSW * 64 * kMaxRG * R * sizeof(C);
-  return kHdr + (size_t)NS * CW * ldn_max * sizeof(C) + 3 * (size_t)R * nJ * sizeof(C) + nx_max + nJ + 32 +
+  return kHdr + (size_t)NS * CW * ldn_max * sizeof(C) + 4 * (size_t)R * nJ * sizeof(C) + nx_max + nJ + 32 +
          2 * (size_t)CL * R * nJ * sizeof(C) + staging + 4 * (size_t)ny_max +
          2 * (size_t)nx_max * sizeof(C) +
-         (size_t)R * (sizeof(DevSlot) + sizeof(SlotCoef) + sizeof(DevGroup)) + 11 * 16;
+         (size_t)R * (sizeof(DevSlot) + sizeof(SlotCoef) + sizeof(DevGroup)) + 12 * 16;
 }
 
 }  // namespace
@@ -847,6 +914,7 @@ cudaError_t launch_front(const FrontArgs& a_in, int max_ny, int max_nx, cudaStre
   }
   const int R = std::min(front_rpad(std::max(1, a.max_slots)), front_rmax(dbl));
   if (a.cluster < 1) a.cluster = 1;
+  if (a.cluster > 4 || max_nx < 5) return cudaErrorInvalidValue;   // clusters of <= 8; two lines per half
   int dev = 0, maxopt = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
@@ -871,11 +939,11 @@ cudaError_t launch_front(const FrontArgs& a_in, int max_ny, int max_nx, cudaStre
   const size_t smem = smem_need<T>(ldn, max_ny, max_nx, R, KSW, a.cluster, CW, NS, split);
   cudaLaunchConfig_t cfg{};
   cudaLaunchAttribute attr[1];
-  cfg.gridDim = dim3((unsigned)(a.item_count * a.cluster));
+  cfg.gridDim = dim3((unsigned)(a.item_count * 2 * a.cluster));
   cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = (unsigned)a.cluster;
+  attr[0].val.clusterDim.x = (unsigned)(2 * a.cluster);   // top and bottom halves
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
