@@ -137,7 +137,7 @@ typedef struct lsw_gmres_report {
   double final_log;    /* last logged relative residual (max over rhs) */
   double true_rel_res; /* ||b - A x|| / ||b|| after the solve, FP64, max over rhs */
   double seconds;      /* wall time of the solve */
-  int precond_applies; /* preconditioner applications (per right-hand side batch) */
+  int precond_applies; /* batched preconditioner applications (summed over sub-batches) */
   double* log;         /* optional caller buffer for the residual log of rhs 0 */
   int log_capacity;
   int log_len;
@@ -192,7 +192,10 @@ lsw_status lsw_assemble_rhs(lsw_ctx* ctx, const double* src_xy_host, const doubl
 
 /* GlobalIterativeSolverGMRES::solve (GlobalIterativeSolverGMRES.cpp:65-203)
  * on device vectors; every right-hand side of the batch is iterated in
- * lockstep and shares each preconditioner launch. */
+ * lockstep and shares each preconditioner launch.  A batch whose Krylov bases
+ * do not fit in free device memory is solved as consecutive sub-batches
+ * (report: iterations and residuals are the maxima over all right-hand sides,
+ * precond_applies the sum over the sub-batches). */
 lsw_status lsw_gmres(lsw_ctx* ctx, const void* b_dev, void* x_dev, int nrhs,
                      const lsw_gmres_opts* opts, lsw_gmres_report* report, void* stream);
 
@@ -200,6 +203,13 @@ lsw_status lsw_gmres(lsw_ctx* ctx, const void* b_dev, void* x_dev, int nrhs,
  * on host buffers: copies b to the device, solves, copies x back. */
 lsw_status lsw_solve_host(lsw_ctx* ctx, const double* b_host, double* x_host, int nrhs,
                           const lsw_gmres_opts* opts, lsw_gmres_report* report, void* stream);
+
+/* Frees the context's solve workspaces: Krylov bases, sweep schedules and
+ * their trace, output and scratch pools, lsw_solve_host's device copies of b
+ * and x (they are rebuilt by the next call that needs them).  Factors and the problem stay resident.  No counterpart
+ * in the reference (its workspaces are per-call Eigen vectors); a serving loop
+ * calls it on idle operators to return device memory. */
+lsw_status lsw_release_workspace(lsw_ctx* ctx);
 
 /* LocalLinearSolver::solve (include/LocalLinearSolver.h:40) for one cell:
  * x = A_cell^-1 b on full cell vectors (nx*ny complex128, local order i*ny+j),

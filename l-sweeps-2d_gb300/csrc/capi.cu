@@ -35,6 +35,11 @@ struct DevBuf {
     return e;
   }
   template <typename X> X* as() const { return reinterpret_cast<X*>(p); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
 };
 
 struct lsw_ctx {
@@ -58,10 +63,13 @@ struct lsw_ctx {
   DevBuf k_basis, k_zbasis, k_tmp, k_tmp2, k_r, k_part, k_small, k_small2, k_nrm;
   // local-solve workspace
   DevBuf ls_items, ls_slots, ls_scratch;
+  // lsw_solve_host's device copies of b and x, kept between calls
+  DevBuf h_b, h_x;
   size_t fixed_bytes = 0;
   long long launches = 0;
   int nsm = 152;
   int max_cluster = 8;
+  int krylov_batch = 0;   // right-hand sides per Krylov sub-batch at most (0: as memory allows)
   // optional per-front timing of one apply
   std::vector<cudaEvent_t>* front_events = nullptr;
 };
@@ -138,10 +146,20 @@ size_t device_bytes(const lsw_ctx* c) {
              c->d_work.bytes + c->d_status.bytes + c->d_traces.bytes + c->d_outs.bytes + c->d_scratch.bytes +
              c->k_basis.bytes + c->k_zbasis.bytes + c->k_tmp.bytes + c->k_tmp2.bytes + c->k_r.bytes +
              c->k_part.bytes + c->k_small.bytes + c->k_small2.bytes + c->k_nrm.bytes + c->ls_items.bytes +
-             c->ls_slots.bytes + c->ls_scratch.bytes;
+             c->ls_slots.bytes + c->ls_scratch.bytes + c->h_b.bytes + c->h_x.bytes;
   for (auto& kv : c->sched_bufs)
     for (int i = 0; i < 3; ++i) b += kv.second[i].bytes;
   return b;
+}
+
+// CTAs per half for a single-cell solve: `cl`, or the next larger size whose
+// launch fits in shared memory
+int fitting_cluster(const lsw_ctx* ctx, int slots, int cl) {
+  const int mask = front_fit_mask(ctx->prec == LSW_PREC_C128, ctx->prec == LSW_PREC_SPLIT, ctx->max_ny,
+                                  ctx->max_nx, slots);
+  for (int c = cl; c <= 4; c *= 2)
+    if (mask & (1 << c)) return c;
+  return cl;   // nothing fits: the launch reports it
 }
 
 lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out) {
@@ -161,6 +179,8 @@ lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out) {
         plan.line_overhead = 2200.0; plan.slot_cost = 0.0; plan.col_cost = 40.0; plan.col_slot_cost = 3.0;
       }
       for (int cl = 1; cl <= 4; cl *= 2) plan.max_clusters[cl] = front_max_clusters(dbl, 2 * cl);
+      for (int r = 1; r <= 16; ++r)
+        plan.fit_mask[r] = front_fit_mask(dbl, ctx->prec == LSW_PREC_SPLIT, ctx->max_ny, ctx->max_nx, r);
       if (plan.max_clusters[1] <= 0) plan.max_clusters[1] = ctx->nsm / 2;
       build_schedule(ctx->cells, ctx->N, nrhs, plan, ctx->LP, sc->fronts, items, slots, groups, ctx->n2);
     } catch (const std::exception& ex) {
@@ -363,6 +383,8 @@ lsw_status lsw_ctx_create(lsw_ctx** out, int device) {
     const int v = std::atoi(ev);
     if (v >= 2 && v <= 8) c->max_cluster = v;
   }
+  // LSW_KRYLOV_BATCH caps the right-hand sides iterated together by lsw_gmres
+  if (const char* ev = std::getenv("LSW_KRYLOV_BATCH")) c->krylov_batch = std::max(0, std::atoi(ev));
   *out = c;
   return LSW_OK;
 }
@@ -646,7 +668,7 @@ lsw_status lsw_local_solve(lsw_ctx* ctx, int cell, const void* b, void* x, int n
   a.max_slots = std::min(rmax, nrhs);
   a.err = ctx->d_status.as<int>() + 1;
   a.split = ctx->prec == LSW_PREC_SPLIT ? 1 : 0;
-  a.cluster = front_cluster(a.item_count, ctx->nsm, ctx->max_cluster);
+  a.cluster = fitting_cluster(ctx, a.max_slots, front_cluster(a.item_count, ctx->nsm, ctx->max_cluster));
   cudaError_t e = dbl ? launch_front<double>(a, ctx->max_ny, ctx->max_nx, st) : launch_front<float>(a, ctx->max_ny, ctx->max_nx, st);
   CK(e, "local solve kernel");
   ctx->launches += 1;
@@ -975,17 +997,57 @@ lsw_status lsw_gmres(lsw_ctx* ctx, const void* b, void* x, int nrhs, const lsw_g
   const auto t0 = std::chrono::steady_clock::now();
   const double2* bb = reinterpret_cast<const double2*>(b);
   double2* xx = reinterpret_cast<double2*>(x);
-  lsw_status s;
-  if (o->mode == LSW_GMRES_REFERENCE) s = gmres_reference(ctx, bb, xx, nrhs, o, rep, st);
-  else if (o->mode == LSW_GMRES_FLEXIBLE) s = gmres_flexible(ctx, bb, xx, nrhs, o, rep, st);
-  else return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "unknown GMRES mode");
-  if (s != LSW_OK) return s;
+  if (o->mode != LSW_GMRES_REFERENCE && o->mode != LSW_GMRES_FLEXIBLE)
+    return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "unknown GMRES mode");
+  // Right-hand sides per Krylov batch.  Every right-hand side of a batch keeps
+  // its whole basis resident (2 m + 1 vectors for FGMRES(m), MaxIter + 1 for
+  // the reference GMRES), so a batch larger than the free device memory holds
+  // is solved as consecutive sub-batches, each still sharing every sweep
+  // launch among its right-hand sides.
+  const long long n2 = ctx->n2;
+  const size_t vec = (size_t)n2 * sizeof(double2);
+  const size_t nvec = o->mode == LSW_GMRES_REFERENCE ? (size_t)o->max_iter + 4 : 2 * (size_t)std::max(1, o->restart) + 4;
+  const size_t per_rhs = nvec * vec + 12 * (size_t)n2 * csize(ctx->prec);   // + sweep pools (outputs, traces)
+  size_t fr = 0, tot = 0;
+  CK(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+  const size_t held = ctx->k_basis.bytes + ctx->k_zbasis.bytes + ctx->k_tmp.bytes + ctx->k_tmp2.bytes;
+  const size_t margin = (size_t)2 << 30;
+  const size_t budget = fr + held > margin ? fr + held - margin : 0;
+  int chunk = (int)std::max<long long>(1, std::min<long long>(nrhs, (long long)(budget / per_rhs)));
+  if (ctx->krylov_batch > 0) chunk = std::min(chunk, ctx->krylov_batch);
+  lsw_gmres_report sub{}, acc{};
+  acc.converged = 1;
   double tr = 0.0;
-  if ((s = true_residual(ctx, bb, xx, nrhs, &tr, st)) != LSW_OK) return s;
+  for (int c0 = 0; c0 < nrhs; c0 += chunk) {
+    const int nv = std::min(chunk, nrhs - c0);
+    sub = lsw_gmres_report{};
+    if (rep && c0 == 0) { sub.log = rep->log; sub.log_capacity = rep->log_capacity; }
+    lsw_status s = o->mode == LSW_GMRES_REFERENCE
+                       ? gmres_reference(ctx, bb + (size_t)c0 * n2, xx + (size_t)c0 * n2, nv, o, &sub, st)
+                       : gmres_flexible(ctx, bb + (size_t)c0 * n2, xx + (size_t)c0 * n2, nv, o, &sub, st);
+    if (s != LSW_OK) return s;
+    double t = 0.0;
+    if ((s = true_residual(ctx, bb + (size_t)c0 * n2, xx + (size_t)c0 * n2, nv, &t, st)) != LSW_OK) return s;
+    tr = std::max(tr, t);
+    acc.iterations = std::max(acc.iterations, sub.iterations);
+    acc.final_log = std::max(acc.final_log, sub.final_log);
+    acc.precond_applies += sub.precond_applies;
+    acc.converged = acc.converged && sub.converged;
+    if (c0 == 0) acc.log_len = sub.log_len;
+  }
+  lsw_status s;
   if ((s = check_kernel_err(ctx, st)) != LSW_OK) return s;
   CK(cudaStreamSynchronize(st), "sync");
   const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-  if (rep) { rep->true_rel_res = tr; rep->seconds = secs; }
+  if (rep) {
+    rep->iterations = acc.iterations;
+    rep->converged = acc.converged;
+    rep->final_log = acc.final_log;
+    rep->precond_applies = acc.precond_applies;
+    rep->log_len = acc.log_len;
+    rep->true_rel_res = tr;
+    rep->seconds = secs;
+  }
   return LSW_OK;
 }
 
@@ -996,7 +1058,8 @@ lsw_status lsw_solve_host(lsw_ctx* ctx, const double* b_host, double* x_host, in
   CK(cudaSetDevice(ctx->device), "cudaSetDevice");
   cudaStream_t st = S(stream);
   const size_t vb = (size_t)nrhs * ctx->n2 * sizeof(double2);
-  DevBuf db, dx;
+  DevBuf& db = ctx->h_b;
+  DevBuf& dx = ctx->h_x;
   CK(db.ensure(vb), "cudaMalloc(b)");
   CK(dx.ensure(vb), "cudaMalloc(x)");
   CK(cudaMemcpyAsync(db.p, b_host, vb, cudaMemcpyHostToDevice, st), "H2D b");
@@ -1004,6 +1067,19 @@ lsw_status lsw_solve_host(lsw_ctx* ctx, const double* b_host, double* x_host, in
   if (s != LSW_OK) return s;
   CK(cudaMemcpyAsync(x_host, dx.p, vb, cudaMemcpyDeviceToHost, st), "D2H x");
   CK(cudaStreamSynchronize(st), "sync");
+  return LSW_OK;
+}
+
+lsw_status lsw_release_workspace(lsw_ctx* ctx) {
+  if (!ctx) return LSW_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  CK(cudaDeviceSynchronize(), "sync");   // no launch may still use the buffers
+  ctx->sched.clear();
+  ctx->sched_bufs.clear();
+  for (DevBuf* b : {&ctx->d_traces, &ctx->d_outs, &ctx->d_scratch, &ctx->k_basis, &ctx->k_zbasis, &ctx->k_tmp,
+                    &ctx->k_tmp2, &ctx->k_r, &ctx->k_part, &ctx->k_small, &ctx->k_small2, &ctx->k_nrm,
+                    &ctx->ls_items, &ctx->ls_slots, &ctx->ls_scratch, &ctx->h_b, &ctx->h_x})
+    b->release();
   return LSW_OK;
 }
 
@@ -1067,7 +1143,7 @@ lsw_status lsw_local_solve_noalloc(lsw_ctx* ctx, int cell, const void* b, void* 
   a.max_slots = std::min(rmax, nrhs);
   a.err = ctx->d_status.as<int>() + 1;
   a.split = ctx->prec == LSW_PREC_SPLIT ? 1 : 0;
-  a.cluster = front_cluster(a.item_count, ctx->nsm, ctx->max_cluster);
+  a.cluster = fitting_cluster(ctx, a.max_slots, front_cluster(a.item_count, ctx->nsm, ctx->max_cluster));
   cudaError_t e = dbl ? launch_front<double>(a, ctx->max_ny, ctx->max_nx, st) : launch_front<float>(a, ctx->max_ny, ctx->max_nx, st);
   CK(e, "local solve kernel");
   ctx->launches += 2;

@@ -327,6 +327,7 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
       for (int cl = 1; cl <= plan.cluster_cap; cl *= 2) {
         const int mc = std::max(1, plan.max_clusters[cl]);
         if (plan.max_clusters[cl] <= 0 && cl > 1) continue;
+        if (!(plan.fit_mask[R] & (1 << cl))) continue;   // shared memory
         const long long waves = (n_items + mc - 1) / mc;
         const double line = plan.line_overhead + plan.slot_cost * R +
                             (plan.col_cost + plan.col_slot_cost * R) * ((ny_max + cl - 1) / cl);
@@ -338,6 +339,7 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
         }
       }
     }
+    if (best_t >= 1e300) throw std::runtime_error("no sweep-front launch shape fits in shared memory");
     Front F{(int)items.size(), 0, 0, 0, best_cl};
     for (auto& kv : f) {
       const int c = kv.first;

@@ -106,6 +106,7 @@ struct FrontPlan {
   // indexed by the CTAs per half (1, 2, 4): resident clusters of twice that many CTAs
   int max_clusters[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   int cluster_cap = 4;       // CTAs per half
+  int fit_mask[17] = {0};    // per padded slot count: bit CL set where the launch fits in shared memory
   int rmax = 16;
   int csize = 8;             // bytes per complex value of the factors
   double line_overhead = 1800.0;
@@ -177,6 +178,8 @@ template <typename T> cudaError_t launch_front(const FrontArgs& a, int max_ny, i
 int front_max_clusters(bool dbl, int cluster);
 int front_rmax(bool dbl);
 int front_rpad(int n);
+// bit CL (1, 2, 4) set where items of `slots` slots on clusters of 2 CL CTAs fit in shared memory
+int front_fit_mask(bool dbl, bool split, int max_ny, int max_nx, int slots);
 // split: write every factor entry as bf16 hi/lo terms; `prev` then holds each
 // cell's previous FP32 block (ny x ldn complex per cell) for the Schur recurrence
 template <typename T> cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* prof,

@@ -44,6 +44,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <type_traits>
 
 namespace lsw {
 
@@ -134,6 +135,56 @@ __device__ __forceinline__ uint2 split_entry(float2 v) {
 
 // block-column owner: CTA g owns the columns [g n/G, (g+1) n/G)
 __device__ __forceinline__ int col_owner(int j, int n, int G) { return ((j + 1) * G - 1) / n; }
+
+// Rank-bt update of the non-pivot rows on columns [cb, ce) of W:
+// c[r] -= sum_t f_t[r] u_t, register-tiled (kRI rows x CJ columns per thread)
+// over NTHR threads; lt = thread index within them.
+template <typename T, int NTHR>
+__device__ __noinline__ void rank_update(const cx_t<T>* __restrict__ Fb, const cx_t<T>* __restrict__ U,
+                                            cx_t<T>* __restrict__ W, const int* __restrict__ pslot, int n,
+                                            int nmax, int ldw, int bt, int cb, int ce, int lt) {
+  using C = cx_t<T>;
+  constexpr int CJ = FacCfg<T>::CJ;
+  constexpr int NTY = NTHR / kTX;
+  const C z = czero<C>();
+  const int tx = lt % kTX, ty = lt / kTX;
+  for (int rb = 0; rb < n; rb += NTY * kRI) {
+    C acc[kRI][CJ];
+#pragma unroll
+    for (int a = 0; a < kRI; ++a)
+#pragma unroll
+      for (int b = 0; b < CJ; ++b) acc[a][b] = z;
+    for (int t = 0; t < bt; ++t) {
+      C fr[kRI], uc[CJ];
+#pragma unroll
+      for (int a = 0; a < kRI; ++a) {
+        const int r = rb + ty + NTY * a;
+        fr[a] = r < n ? Fb[(size_t)t * nmax + r] : z;
+      }
+#pragma unroll
+      for (int b = 0; b < CJ; ++b) {
+        const int cc = cb + tx + kTX * b;
+        uc[b] = cc < ce ? U[(size_t)t * ldw + cc] : z;
+      }
+#pragma unroll
+      for (int a = 0; a < kRI; ++a)
+#pragma unroll
+        for (int b = 0; b < CJ; ++b) cfma(acc[a][b], fr[a], uc[b]);
+    }
+#pragma unroll
+    for (int a = 0; a < kRI; ++a) {
+      const int r = rb + ty + NTY * a;
+      if (r >= n || pslot[r] >= 0) continue;
+#pragma unroll
+      for (int b = 0; b < CJ; ++b) {
+        const int cc = cb + tx + kTX * b;
+        if (cc >= ce) continue;
+        C* w = W + (size_t)r * ldw + cc;
+        *w = csub(*w, acc[a][b]);
+      }
+    }
+  }
+}
 
 template <typename T>
 __global__ void __launch_bounds__(kFT, 1)
@@ -262,187 +313,196 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
     __syncthreads();
 
     // ---- blocked Gauss-Jordan over the pivot columns in order ----
-    int blk = 0;
-    for (int k0 = 0; k0 < n; ++blk) {
-      const int o = col_owner(k0, n, G);
-      const int oend = (o + 1) * n / G;
-      const int k1 = min(k0 + kB, oend), bt = k1 - k0, buf = blk & 1;
+    // Panel of block [k0, k1): the classic steps on those columns of my W,
+    // one row per thread of warps 0 .. kMaxN/32 - 1, the row's panel part in
+    // registers (named barrier 1 among those warps); records f_t, the pivots
+    // and the reciprocals in buffer `buf`.
+    auto panel = [&](int k0, int k1, int buf) {
+      const int bt = k1 - k0;
       C* Fb = F + (size_t)buf * kB * nmax;
       int* pbb = pb + buf * kB;
       C* ivb = invv + buf * kB;
-
-      if ((int)g == o && tid < kMaxN) {
-        // panel: the classic steps on columns [k0, k1) of my W, one row per
-        // thread of the first kMaxN / 32 warps, the row's panel part in
-        // registers (named barrier 1 among those warps)
-        const int r = tid;
-        const bool live = r < n;
-        const int pc = k0 - c0;
-        C row[kB];
+      const int r = tid;
+      const bool live = r < n;
+      const int pc = k0 - c0;
+      C row[kB];
 #pragma unroll
-        for (int q = 0; q < kB; ++q) row[q] = (live && q < bt) ? W[(size_t)r * ldw + pc + q] : z;
-        bool mine_used = live ? (used[r] != 0) : true;
+      for (int q = 0; q < kB; ++q) row[q] = (live && q < bt) ? W[(size_t)r * ldw + pc + q] : z;
+      bool mine_used = live ? (used[r] != 0) : true;
 #pragma unroll
-        for (int t = 0; t < kB; ++t) {
-          if (t >= bt) break;
-          const C v = row[t];
-          if (live) Fb[(size_t)t * nmax + r] = v;
-          T best = (live && !mine_used) ? abs2(v) : (T)-1;
-          int bi = (live && !mine_used) ? r : n;
+      for (int t = 0; t < kB; ++t) {
+        if (t >= bt) break;
+        const C v = row[t];
+        if (live) Fb[(size_t)t * nmax + r] = v;
+        T best = (live && !mine_used) ? abs2(v) : (T)-1;
+        int bi = (live && !mine_used) ? r : n;
 #pragma unroll
-          for (int off = 16; off > 0; off >>= 1) {
-            const T ob = __shfl_down_sync(0xffffffffu, best, off);
-            const int oi = __shfl_down_sync(0xffffffffu, bi, off);
-            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-          }
-          if (lane == 0) { wbest[warp] = best; wbi[warp] = bi; }
-          named_sync(1, kMaxN);
-          best = wbest[0];
-          bi = wbi[0];
+        for (int off = 16; off > 0; off >>= 1) {
+          const T ob = __shfl_down_sync(0xffffffffu, best, off);
+          const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+          if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        if (lane == 0) { wbest[warp] = best; wbi[warp] = bi; }
+        named_sync(1, kMaxN);
+        best = wbest[0];
+        bi = wbi[0];
 #pragma unroll
-          for (int w = 1; w < kMaxN / 32; ++w) {
-            const T ob = wbest[w];
-            const int oi = wbi[w];
-            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-          }
-          if (!(best > (T)0) || !isfinite((double)best) || bi >= n) {
-            if (r == 0) atomicOr(status, 1);
-            // keep going with the first unpivoted row so the kernel terminates normally
-            bi = 0;
-            while (bi < n && used[bi]) ++bi;
-            if (bi >= n) bi = 0;
-          }
-          const int p = bi;
-          if (r == p) {
-            const C inv = crcp(v);
-            mine_used = true;
-            used[r] = 1;
-            piv[k0 + t] = r;
-            pbb[t] = r;
-            ivb[t] = inv;
+        for (int w = 1; w < kMaxN / 32; ++w) {
+          const T ob = wbest[w];
+          const int oi = wbi[w];
+          if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        if (!(best > (T)0) || !isfinite(best) || bi >= n) {
+          if (r == 0) atomicOr(status, 1);
+          // keep going with the first unpivoted row so the kernel terminates normally
+          bi = 0;
+          while (bi < n && used[bi]) ++bi;
+          if (bi >= n) bi = 0;
+        }
+        const int p = bi;
+        if (r == p) {
+          const C inv = crcp(v);
+          mine_used = true;
+          used[r] = 1;
+          piv[k0 + t] = r;
+          pbb[t] = r;
+          ivb[t] = inv;
 #pragma unroll
-            for (int q = 0; q < kB; ++q) {
-              if (q < bt) {
-                row[q] = (q == t) ? inv : cmul(row[q], inv);
-                rowp[q] = row[q];
-              }
-            }
-          }
-          named_sync(1, kMaxN);
-          if (live && r != p) {
-            const C inv = ivb[t];
-#pragma unroll
-            for (int q = 0; q < kB; ++q) {
-              if (q < bt) {
-                if (q == t) row[q] = cneg(cmul(v, inv));
-                else cfms(row[q], v, rowp[q]);
-              }
+          for (int q = 0; q < kB; ++q) {
+            if (q < bt) {
+              row[q] = (q == t) ? inv : cmul(row[q], inv);
+              rowp[q] = row[q];
             }
           }
         }
+        named_sync(1, kMaxN);
+        if (live && r != p) {
+          const C inv = ivb[t];
 #pragma unroll
-        for (int q = 0; q < kB; ++q)
-          if (live && q < bt) W[(size_t)r * ldw + pc + q] = row[q];
-      }
-      if (!csync()) return;
-      if ((int)g != o) {
-        // the panel owner's columns f_t, pivots and reciprocals
-        for (int e = tid; e < bt * n; e += kFT) {
-          const int t = e / n, r = e - t * n;
-          Fb[(size_t)t * nmax + r] = ld_remote(Fb + (size_t)t * nmax + r, (unsigned)o);
-        }
-        if (tid < bt) {
-          const int p = ld_remote(pbb + tid, (unsigned)o);
-          pbb[tid] = p;
-          ivb[tid] = ld_remote(ivb + tid, (unsigned)o);
-          used[p] = 1;
-          piv[k0 + tid] = p;
-        }
-        __syncthreads();
-      }
-      if (tid < bt) pslot[pbb[tid]] = tid;
-      __syncthreads();
-
-      // (a) u = M1 g per column, with M1 = (D + L)^{-1} (D = diag f_t[p_t],
-      // L[t][s] = f_s[p_t], s < t) formed once per block by one warp, lane j
-      // solving for column j; then the pivot rows' final values
-      // c[p_t] = u_t - sum_{s>t} f_s[p_t] u_s
-      const int pk0 = ((int)g == o) ? k0 - c0 : -1;   // my panel columns [pk0, pk0 + bt), if any
-      if (warp == 0 && lane < bt) {
-        C m[kB];
-#pragma unroll
-        for (int t = 0; t < kB; ++t) {
-          if (t < bt) {
-            C a = (t == lane) ? to_c(make_double2(1.0, 0.0), z) : z;
-#pragma unroll
-            for (int s2 = 0; s2 < kB; ++s2)
-              if (s2 < t) cfms(a, Fb[(size_t)s2 * nmax + pbb[t]], m[s2]);
-            m[t] = cmul(a, ivb[t]);
-            M1[t * kB + lane] = m[t];
+          for (int q = 0; q < kB; ++q) {
+            if (q < bt) {
+              if (q == t) row[q] = cneg(cmul(v, inv));
+              else cfms(row[q], v, rowp[q]);
+            }
           }
         }
       }
-      __syncthreads();
-      for (int e = tid; e < bt * nc; e += kFT) {
-        const int t = e / nc, cc = e - t * nc;
-        if (pk0 >= 0 && cc >= pk0 && cc < pk0 + bt) continue;
+#pragma unroll
+      for (int q = 0; q < kB; ++q)
+        if (live && q < bt) W[(size_t)r * ldw + pc + q] = row[q];
+    };
+
+    // Block of bt pivots (buffer `buf`) on my columns [cb, ce) except
+    // [x0, x1): u = M1 g per column, the pivot rows' final values
+    // c[p_t] = u_t - sum_{s>t} f_s[p_t] u_s, and the rank-bt update
+    // c[r] -= sum_t f_t[r] u_t of the other rows.  All kFT threads
+    // (NTHR = kFT, CTA barrier) or the kFT - kMaxN threads past the panel
+    // warps (named barrier 2) take part.
+    auto finish = [&](auto nthr_c, int bt, int buf, int cb, int ce, int x0, int x1) {
+      constexpr int NTHR = decltype(nthr_c)::value;
+      const int lt = tid - (kFT - NTHR);
+      const C* Fb = F + (size_t)buf * kB * nmax;
+      const int* pbb = pb + buf * kB;
+      // two contiguous column ranges [cb, xa) and [xb, ce)
+      const int xa = max(cb, min(x0, ce)), xb = max(xa, min(x1, ce));
+      const int na = xa - cb, ncols = na + (ce - xb);
+      auto colof = [&](int i) { return i < na ? cb + i : xb + (i - na); };
+      for (int e = lt; e < bt * ncols; e += NTHR) {
+        const int t = e / ncols, cc = colof(e - t * ncols);
         C a = z;
         for (int s2 = 0; s2 <= t; ++s2) cfma(a, M1[t * kB + s2], W[(size_t)pbb[s2] * ldw + cc]);
         U[(size_t)t * ldw + cc] = a;
       }
-      __syncthreads();
-      for (int e = tid; e < bt * nc; e += kFT) {
-        const int t = e / nc, cc = e - t * nc;
-        if (pk0 >= 0 && cc >= pk0 && cc < pk0 + bt) continue;
+      if (NTHR == kFT) __syncthreads();
+      else named_sync(2, NTHR);
+      // pivot rows, then (no barrier: disjoint rows, reading only U and F) the others
+      for (int e = lt; e < bt * ncols; e += NTHR) {
+        const int t = e / ncols, cc = colof(e - t * ncols);
         C a = U[(size_t)t * ldw + cc];
         const int pt = pbb[t];
         for (int s2 = t + 1; s2 < bt; ++s2) cfms(a, Fb[(size_t)s2 * nmax + pt], U[(size_t)s2 * ldw + cc]);
         W[(size_t)pt * ldw + cc] = a;
       }
-      __syncthreads();
+      if (na > 0) rank_update<T, NTHR>(Fb, U, W, pslot, n, nmax, ldw, bt, cb, xa, lt);
+      if (ce > xb) rank_update<T, NTHR>(Fb, U, W, pslot, n, nmax, ldw, bt, xb, ce, lt);
+    };
+    using AllThreads = std::integral_constant<int, kFT>;
+    using RestThreads = std::integral_constant<int, kFT - kMaxN>;
 
-      // (b) rank-bt update of the other rows: c[r] -= sum_t f_t[r] u_t
-      {
-        const int tx = tid % kTX, ty = tid / kTX;
-        C acc[kRI][CJ];
-#pragma unroll
-        for (int a = 0; a < kRI; ++a)
-#pragma unroll
-          for (int b = 0; b < CJ; ++b) acc[a][b] = z;
-        for (int t = 0; t < bt; ++t) {
-          C fr[kRI], uc[CJ];
-#pragma unroll
-          for (int a = 0; a < kRI; ++a) {
-            const int r = ty + kTY * a;
-            fr[a] = r < n ? Fb[(size_t)t * nmax + r] : z;
+    // Look-ahead: the owner of the next block's columns finishes the current
+    // block on those columns first, then factors the next panel on warps
+    // 0 .. kMaxN/32 - 1 while its other warps finish the current block on the
+    // rest of its columns; the cluster sync that follows publishes the panel.
+    // Iteration blk = -1 has no current block and only factors the first panel.
+    int k0 = 0, k1 = 0;   // current block [k0, k1); the next one starts at k1
+    for (int blk = -1;; ++blk) {
+      const bool cur = blk >= 0;
+      const int o = cur ? col_owner(k0, n, G) : -1;
+      const int bt = k1 - k0, buf = blk & 1;
+      C* Fb = F + (size_t)buf * kB * nmax;
+      int* pbb = pb + buf * kB;
+      C* ivb = invv + buf * kB;
+      const bool more = k1 < n;
+      const int o2 = more ? col_owner(k1, n, G) : -1;
+      const int k2 = more ? min(k1 + kB, (o2 + 1) * n / G) : k1;
+
+      if (cur) {
+        if (!csync()) return;
+        if ((int)g != o) {
+          // the panel owner's columns f_t, pivots and reciprocals
+          for (int e = tid; e < bt * n; e += kFT) {
+            const int t = e / n, r = e - t * n;
+            Fb[(size_t)t * nmax + r] = ld_remote(Fb + (size_t)t * nmax + r, (unsigned)o);
           }
-#pragma unroll
-          for (int b = 0; b < CJ; ++b) {
-            const int cc = tx + kTX * b;
-            uc[b] = cc < nc ? U[(size_t)t * ldw + cc] : z;
+          if (tid < bt) {
+            const int p = ld_remote(pbb + tid, (unsigned)o);
+            pbb[tid] = p;
+            ivb[tid] = ld_remote(ivb + tid, (unsigned)o);
+            used[p] = 1;
+            piv[k0 + tid] = p;
           }
-#pragma unroll
-          for (int a = 0; a < kRI; ++a)
-#pragma unroll
-            for (int b = 0; b < CJ; ++b) cfma(acc[a][b], fr[a], uc[b]);
+          __syncthreads();
         }
+        if (tid < bt) pslot[pbb[tid]] = tid;
+        // M1 = (D + L)^{-1} (D = diag f_t[p_t], L[t][s] = f_s[p_t], s < t),
+        // formed once per block by one warp, lane j solving for column j
+        if (warp == 0 && lane < bt) {
+          C m[kB];
 #pragma unroll
-        for (int a = 0; a < kRI; ++a) {
-          const int r = ty + kTY * a;
-          if (r >= n || pslot[r] >= 0) continue;
+          for (int t = 0; t < kB; ++t) {
+            if (t < bt) {
+              C a = (t == lane) ? to_c(make_double2(1.0, 0.0), z) : z;
 #pragma unroll
-          for (int b = 0; b < CJ; ++b) {
-            const int cc = tx + kTX * b;
-            if (cc >= nc || (pk0 >= 0 && cc >= pk0 && cc < pk0 + bt)) continue;
-            C* w = W + (size_t)r * ldw + cc;
-            *w = csub(*w, acc[a][b]);
+              for (int s2 = 0; s2 < kB; ++s2)
+                if (s2 < t) cfms(a, Fb[(size_t)s2 * nmax + pbb[t]], m[s2]);
+              m[t] = cmul(a, ivb[t]);
+              M1[t * kB + lane] = m[t];
+            }
           }
         }
+        __syncthreads();
+      }
+      const bool look = more && (int)g == o2;
+      const int pk0 = (cur && (int)g == o) ? k0 - c0 : -1;   // my panel columns [pk0, pk0 + bt), if any
+      const int n0 = k1 - c0, n1 = k2 - c0;                  // the next panel's columns, if mine
+      if (cur && look) {
+        finish(AllThreads{}, bt, buf, n0, n1, -1, -1);
+        __syncthreads();
+      }
+      if (look && tid < kMaxN) {
+        panel(k1, k2, (blk + 1) & 1);
+      } else if (cur) {
+        if (look) finish(RestThreads{}, bt, buf, 0, nc, pk0 >= 0 ? pk0 : n0, n1);
+        else finish(AllThreads{}, bt, buf, 0, nc, pk0, pk0 >= 0 ? pk0 + bt : -1);
       }
       __syncthreads();
-      if (tid < bt) pslot[pbb[tid]] = -1;
-      __syncthreads();
+      if (cur) {
+        if (tid < bt) pslot[pbb[tid]] = -1;
+        __syncthreads();
+      }
+      if (!more) break;
       k0 = k1;
+      k1 = k2;
     }
 
     // ---- unscramble my columns: output column piv[c] holds W[piv[i]][c] ----

@@ -900,6 +900,55 @@ size_t smem_need(int ldn_max, int ny_max, int nx_max, int R, int KSW, int CL, in
 int front_rmax(bool dbl) { return dbl ? 8 : 16; }
 int front_rpad(int n) { return n <= 1 ? 1 : n <= 2 ? 2 : n <= 4 ? 4 : n <= 8 ? 8 : n <= 12 ? 12 : 16; }
 
+namespace {
+
+// The launch shape of a front: column slices, chunk width and ring depth for
+// R slots on clusters of 2 CL CTAs; false if nothing fits in shared memory.
+template <typename T>
+bool front_shape(int max_ny, int max_nx, int R, int CL, bool split, int maxopt, int* ldn_out, int* ksw_out,
+                 int* cw_out, int* ns_out, size_t* smem_out) {
+  int ldn = (max_ny + 3) & ~3;
+  if (split) {   // the split factor layout's column stride (4 mod 8)
+    ldn = max_ny;
+    while (ldn % 8 != 4) ++ldn;
+  }
+  // largest chunk (columns, multiple of 8, <= ~64 KB) and then the deepest ring that fit
+  const int nJmax = (max_ny + CL - 1) / CL;
+  // column slices: as many as keep >= 4 columns per slice and the slices'
+  // partial-sum staging (KSW x 192 x R) within 64 KB
+  int KSW = kMaxKSW;
+  while (KSW > 1 && (split || nJmax < 4 * KSW || (size_t)KSW * 64 * kMaxRG * R * sizeof(cx_t<T>) > 65536)) --KSW;
+  const int cwmax = (int)std::min<size_t>(((size_t)65536 / ((size_t)ldn * sizeof(cx_t<T>))) & ~size_t(7),
+                                          (size_t)((nJmax + 7) & ~7));
+  int CW = std::max(8, cwmax), NS = 0;
+  for (; CW >= 8; CW -= 8) {
+    for (NS = 4; NS >= 2; --NS)
+      if (smem_need<T>(ldn, max_ny, max_nx, R, KSW, CL, CW, NS, split) <= (size_t)maxopt) break;
+    if (NS >= 2) break;
+  }
+  if (CW < 8) return false;
+  *ldn_out = ldn; *ksw_out = KSW; *cw_out = CW; *ns_out = NS;
+  *smem_out = smem_need<T>(ldn, max_ny, max_nx, R, KSW, CL, CW, NS, split);
+  return true;
+}
+
+}  // namespace
+
+int front_fit_mask(bool dbl, bool split, int max_ny, int max_nx, int slots) {
+  int dev = 0, maxopt = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const int R = std::min(front_rpad(std::max(1, slots)), front_rmax(dbl));
+  int mask = 0, ldn, ksw, cw, ns;
+  size_t smem;
+  for (int cl = 1; cl <= 4; cl *= 2) {
+    const bool ok = dbl ? front_shape<double>(max_ny, max_nx, R, cl, split, maxopt, &ldn, &ksw, &cw, &ns, &smem)
+                        : front_shape<float>(max_ny, max_nx, R, cl, split, maxopt, &ldn, &ksw, &cw, &ns, &smem);
+    if (ok) mask |= 1 << cl;
+  }
+  return mask;
+}
+
 template <typename T>
 cudaError_t launch_front(const FrontArgs& a_in, int max_ny, int max_nx, cudaStream_t st) {
   if (a_in.item_count <= 0) return cudaSuccess;
@@ -907,36 +956,19 @@ cudaError_t launch_front(const FrontArgs& a_in, int max_ny, int max_nx, cudaStre
   const bool dbl = sizeof(T) == 8;
   const bool split = a.split != 0;
   if (split && dbl) return cudaErrorInvalidValue;
-  int ldn = (max_ny + 3) & ~3;
-  if (split) {   // the split factor layout's column stride (4 mod 8)
-    ldn = max_ny;
-    while (ldn % 8 != 4) ++ldn;
-  }
   const int R = std::min(front_rpad(std::max(1, a.max_slots)), front_rmax(dbl));
   if (a.cluster < 1) a.cluster = 1;
   if (a.cluster > 4 || max_nx < 5) return cudaErrorInvalidValue;   // clusters of <= 8; two lines per half
   int dev = 0, maxopt = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  // largest chunk (columns, multiple of 8, <= ~64 KB) and then the deepest ring that fit
-  const int nJmax = (max_ny + a.cluster - 1) / a.cluster;
-  // column slices: as many as keep >= 4 columns per slice and the slices'
-  // partial-sum staging (KSW x 192 x R) within 64 KB
-  int KSW = kMaxKSW;
-  while (KSW > 1 && (split || nJmax < 4 * KSW || (size_t)KSW * 64 * kMaxRG * R * sizeof(cx_t<T>) > 65536)) --KSW;
+  int ldn = 0, KSW = 0, CW = 0, NS = 0;
+  size_t smem = 0;
+  if (!front_shape<T>(max_ny, max_nx, R, a.cluster, split, maxopt, &ldn, &KSW, &CW, &NS, &smem))
+    return cudaErrorInvalidConfiguration;
   a.ksw = KSW;
-  const int cwmax = (int)std::min<size_t>(((size_t)65536 / ((size_t)ldn * sizeof(cx_t<T>))) & ~size_t(7),
-                                          (size_t)((nJmax + 7) & ~7));
-  int CW = std::max(8, cwmax), NS = 0;
-  for (; CW >= 8; CW -= 8) {
-    for (NS = 4; NS >= 2; --NS)
-      if (smem_need<T>(ldn, max_ny, max_nx, R, KSW, a.cluster, CW, NS, split) <= (size_t)maxopt) break;
-    if (NS >= 2) break;
-  }
-  if (CW < 8) return cudaErrorInvalidConfiguration;
   a.stages = NS;
   a.chunk = CW;
-  const size_t smem = smem_need<T>(ldn, max_ny, max_nx, R, KSW, a.cluster, CW, NS, split);
   cudaLaunchConfig_t cfg{};
   cudaLaunchAttribute attr[1];
   cfg.gridDim = dim3((unsigned)(a.item_count * 2 * a.cluster));

@@ -21,7 +21,7 @@ EXPORTS = [
     "lsw_ctx_create", "lsw_ctx_destroy", "lsw_status_string", "lsw_ctx_last_error", "lsw_geometry_cell",
     "lsw_problem_setup", "lsw_problem_info_get", "lsw_cell_info_get", "lsw_factorize", "lsw_apply_precond",
     "lsw_apply_A", "lsw_assemble_rhs", "lsw_gmres", "lsw_solve_host", "lsw_local_solve",
-    "lsw_apply_precond_profiled", "lsw_local_solve_noalloc",
+    "lsw_apply_precond_profiled", "lsw_local_solve_noalloc", "lsw_release_workspace",
 ]
 
 
@@ -102,6 +102,7 @@ def lib() -> C.CDLL:
         "lsw_local_solve": (i, [vp, i, vp, vp, i, vp]),
         "lsw_apply_precond_profiled": (i, [vp, vp, vp, i, vp, C.POINTER(ApplyProfile)]),
         "lsw_local_solve_noalloc": (i, [vp, i, vp, vp, i, vp]),
+        "lsw_release_workspace": (i, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

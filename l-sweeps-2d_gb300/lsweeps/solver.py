@@ -93,6 +93,10 @@ class Solver:
     def factorize(self, stream=None):
         capi.check(self.L.lsw_factorize(self.ctx, _stream_ptr(stream)), self.ctx)
 
+    def release_workspace(self):
+        """Free the Krylov bases and sweep pools (lsw_release_workspace); the factors stay."""
+        capi.check(self.L.lsw_release_workspace(self.ctx), self.ctx)
+
     def apply_precond(self, x, out=None, stream=None):
         torch = _torch()
         nr = self._vec(x)
@@ -145,11 +149,15 @@ class Solver:
                               rep.precond_applies, [logbuf[i] for i in range(rep.log_len)])
 
     def solve_host(self, b_host: np.ndarray, mode: str = "flexible", tol: float = 1e-6, max_iter: int = 200,
-                   restart: int = 30, stream=None):
-        """GlobalIterativeSolver::solve on host buffers (copies included)."""
+                   restart: int = 30, stream=None, x_host: np.ndarray | None = None):
+        """GlobalIterativeSolver::solve on host buffers (copies included); x_host:
+        an optional (pinned) output buffer of b's size."""
         b = np.ascontiguousarray(b_host, dtype=np.complex128)
         nr = b.size // self.n2
-        x = np.empty_like(b)
+        if x_host is not None and (x_host.dtype != np.complex128 or x_host.size != b.size
+                                   or not x_host.flags.c_contiguous):
+            raise ValueError("x_host must be a contiguous complex128 array of b's size")
+        x = np.empty_like(b) if x_host is None else x_host
         opts = capi.GmresOpts(capi.GMRES_MODE[mode], tol, max_iter, restart, 0)
         rep = capi.GmresReport()
         capi.check(self.L.lsw_solve_host(self.ctx, b.ctypes.data_as(C.POINTER(C.c_double)),
