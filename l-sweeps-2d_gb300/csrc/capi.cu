@@ -70,6 +70,7 @@ struct lsw_ctx {
   int nsm = 152;
   int max_cluster = 8;
   int krylov_batch = 0;   // right-hand sides per Krylov sub-batch at most (0: as memory allows)
+  bool factor_lookahead = true;
   // optional per-front timing of one apply
   std::vector<cudaEvent_t>* front_events = nullptr;
 };
@@ -385,6 +386,8 @@ lsw_status lsw_ctx_create(lsw_ctx** out, int device) {
   }
   // LSW_KRYLOV_BATCH caps the right-hand sides iterated together by lsw_gmres
   if (const char* ev = std::getenv("LSW_KRYLOV_BATCH")) c->krylov_batch = std::max(0, std::atoi(ev));
+  // LSW_FACTOR_LOOKAHEAD=0 factors each panel after the whole previous update
+  if (const char* ev = std::getenv("LSW_FACTOR_LOOKAHEAD")) c->factor_lookahead = std::atoi(ev) != 0;
   *out = c;
   return LSW_OK;
 }
@@ -501,10 +504,12 @@ lsw_status lsw_factorize(lsw_ctx* ctx, void* stream) {
   cudaError_t e = ctx->prec != LSW_PREC_C128
                       ? launch_factorize<float>(ctx->d_cells.as<DevCell>(), ctx->ncell, ctx->d_prof.as<double2>(),
                                                 ctx->d_m.as<double>(), ctx->n_dof, w2, ctx->d_fac.p, ctx->d_work.p,
-                                                ctx->max_ny, ctx->d_status.as<int>(), st, ctx->prec == LSW_PREC_SPLIT)
+                                                ctx->max_ny, ctx->d_status.as<int>(), st, ctx->prec == LSW_PREC_SPLIT,
+                                                ctx->factor_lookahead)
                       : launch_factorize<double>(ctx->d_cells.as<DevCell>(), ctx->ncell, ctx->d_prof.as<double2>(),
                                                  ctx->d_m.as<double>(), ctx->n_dof, w2, ctx->d_fac.p, ctx->d_work.p,
-                                                 ctx->max_ny, ctx->d_status.as<int>(), st);
+                                                 ctx->max_ny, ctx->d_status.as<int>(), st, false,
+                                                 false);   // complex128: the update dominates, no overlap
   CK(e, "factorize kernel");
   int status = 0;
   CK(cudaMemcpyAsync(&status, ctx->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H status");

@@ -180,12 +180,14 @@ int front_rmax(bool dbl);
 int front_rpad(int n);
 // bit CL (1, 2, 4) set where items of `slots` slots on clusters of 2 CL CTAs fit in shared memory
 int front_fit_mask(bool dbl, bool split, int max_ny, int max_nx, int slots);
-// split: write every factor entry as bf16 hi/lo terms; `prev` then holds each
-// cell's previous FP32 block (ny x ldn complex per cell) for the Schur recurrence
+// split: write every factor entry as bf16 hi/lo terms; `prev` then holds the
+// previous FP32 block of each cell's two half chains (2 x ny x ldn complex per
+// cell) for the Schur recurrences.  lookahead: factor each next panel while
+// the current block's update runs on the other warps.
 template <typename T> cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* prof,
                                                    const double* mgrid, int n_dof, double omega2,
                                                    void* fac, void* prev, int max_ny, int* status,
-                                                   cudaStream_t st, bool split = false);
+                                                   cudaStream_t st, bool split = false, bool lookahead = true);
 size_t factor_smem_bytes(int ny, bool dbl);
 
 cudaError_t launch_apply_A(const double2* x, double2* y, int nrhs, int n_dof, const double2* gprof,

@@ -137,14 +137,13 @@ __device__ __forceinline__ uint2 split_entry(float2 v) {
 __device__ __forceinline__ int col_owner(int j, int n, int G) { return ((j + 1) * G - 1) / n; }
 
 // Rank-bt update of the non-pivot rows on columns [cb, ce) of W:
-// c[r] -= sum_t f_t[r] u_t, register-tiled (kRI rows x CJ columns per thread)
-// over NTHR threads; lt = thread index within them.
-template <typename T, int NTHR>
-__device__ __noinline__ void rank_update(const cx_t<T>* __restrict__ Fb, const cx_t<T>* __restrict__ U,
+// c[r] -= sum_t f_t[r] u_t, register-tiled (kRI rows x CJ columns per thread,
+// kTX x CJ columns per pass) over NTHR threads; lt = thread index within them.
+template <typename T, int NTHR, int CJ>
+__device__ __forceinline__ void rank_update_body(const cx_t<T>* __restrict__ Fb, const cx_t<T>* __restrict__ U,
                                             cx_t<T>* __restrict__ W, const int* __restrict__ pslot, int n,
                                             int nmax, int ldw, int bt, int cb, int ce, int lt) {
   using C = cx_t<T>;
-  constexpr int CJ = FacCfg<T>::CJ;
   constexpr int NTY = NTHR / kTX;
   const C z = czero<C>();
   const int tx = lt % kTX, ty = lt / kTX;
@@ -186,12 +185,28 @@ __device__ __noinline__ void rank_update(const cx_t<T>* __restrict__ Fb, const c
   }
 }
 
+// complex64: a separate function, so that the kernel's other paths keep their
+// registers; complex128 (bound by FP64 throughput): inlined
+template <typename T, int NTHR, int CJ>
+__device__ __noinline__ void rank_update_call(const cx_t<T>* __restrict__ Fb, const cx_t<T>* __restrict__ U,
+                                                 cx_t<T>* __restrict__ W, const int* __restrict__ pslot, int n,
+                                                 int nmax, int ldw, int bt, int cb, int ce, int lt) {
+  rank_update_body<T, NTHR, CJ>(Fb, U, W, pslot, n, nmax, ldw, bt, cb, ce, lt);
+}
+template <typename T, int NTHR, int CJ>
+__device__ __forceinline__ void rank_update(const cx_t<T>* __restrict__ Fb, const cx_t<T>* __restrict__ U,
+                                            cx_t<T>* __restrict__ W, const int* __restrict__ pslot, int n,
+                                            int nmax, int ldw, int bt, int cb, int ce, int lt) {
+  if constexpr (sizeof(T) == 4) rank_update_call<T, NTHR, CJ>(Fb, U, W, pslot, n, nmax, ldw, bt, cb, ce, lt);
+  else rank_update_body<T, NTHR, CJ>(Fb, U, W, pslot, n, nmax, ldw, bt, cb, ce, lt);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kFT, 1)
 k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
             const double* __restrict__ mgrid, int n_dof, double omega2, cx_t<T>* __restrict__ fac,
-            cx_t<T>* __restrict__ prev, long long prev_stride, int split, int middle, int G, int nmax, int ldw,
-            int* status) {
+            cx_t<T>* __restrict__ prev, long long prev_stride, int split, int middle, int lookahead, int G,
+            int nmax, int ldw, int* status) {
   using C = cx_t<T>;
   constexpr int CJ = FacCfg<T>::CJ;
   constexpr int kB = FacCfg<T>::B;
@@ -215,19 +230,17 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
   // ---- shared layout (identical in every CTA of the cluster) ----
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 8);
-  int* sp = reinterpret_cast<int*>(smem + 12);
-  T* wbest = reinterpret_cast<T*>(smem + 16);                 // [16]
-  int* wbi = reinterpret_cast<int*>(smem + 16 + 16 * 8);      // [16]
+  unsigned* wkey = reinterpret_cast<unsigned*>(smem + 16);    // [2][8] per-warp pivot keys by step parity
   int* used = reinterpret_cast<int*>(smem + 256);             // [nmax]
   int* piv = used + kMaxN;                                     // [nmax]
   int* pslot = piv + kMaxN;                                    // [nmax] block pivot slot of a row, -1 if none
   int* pb = pslot + kMaxN;                                     // [2][kB]
   C* invv = reinterpret_cast<C*>(pb + 2 * kB);                 // [2][kB]
-  C* rowp = invv + 2 * kB;                                     // [kB]
-  C* M1 = rowp + kB;                                           // [kB][kB]
+  C* M1 = invv + 2 * kB;                                       // [kB][kB]
   C* F = M1 + kB * kB;                                         // [2][kB][nmax]
   C* U = F + 2 * kB * nmax;                                    // [kB][ldw]
   C* W = U + kB * ldw;                                         // [nmax][ldw], my columns
+  C* RowB = W + (size_t)nmax * ldw;                            // [2][kB][kMaxN] panel rows by step parity
 
   const double2* px = prof + cl.prof_off;  // lo_x, hi_x, dg_x, lo_y, hi_y, dg_y
   const double2* py = px + 3 * nx;
@@ -313,18 +326,25 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
     __syncthreads();
 
     // ---- blocked Gauss-Jordan over the pivot columns in order ----
-    // Panel of block [k0, k1): the classic steps on those columns of my W,
-    // one row per thread of warps 0 .. kMaxN/32 - 1, the row's panel part in
-    // registers (named barrier 1 among those warps); records f_t, the pivots
-    // and the reciprocals in buffer `buf`.
+    // Panel of block [k0, k1): the classic Gauss-Jordan steps on those columns of
+    // my W (pc = k0 - first column of mine), one row per thread of warps
+    // 0 .. kMaxN/32 - 1, the row's panel part in registers; records f_t, the
+    // pivots and the reciprocals in buffer `buf`.  Each step publishes every row's
+    // panel values (RowB, double-buffered by step parity, so a fast thread's next
+    // step cannot overwrite a row a slow thread still reads) and its pivot key
+    // before one named barrier; after it every thread picks the pivot row and
+    // applies the step itself.  Pivot key: the bits of |v|^2 as float (monotone
+    // for non-negative values) with the low byte replaced by 255 - row, so the
+    // warp maximum (one redux) is the largest magnitude, ties (to 2^-15) going to
+    // the lowest row; used rows have key 0.
     auto panel = [&](int k0, int k1, int buf) {
+      const int pc = k0 - c0;
       const int bt = k1 - k0;
       C* Fb = F + (size_t)buf * kB * nmax;
       int* pbb = pb + buf * kB;
       C* ivb = invv + buf * kB;
       const int r = tid;
       const bool live = r < n;
-      const int pc = k0 - c0;
       C row[kB];
 #pragma unroll
       for (int q = 0; q < kB; ++q) row[q] = (live && q < bt) ? W[(size_t)r * ldw + pc + q] : z;
@@ -332,57 +352,47 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
 #pragma unroll
       for (int t = 0; t < kB; ++t) {
         if (t >= bt) break;
+        C* RB = RowB + (size_t)(t & 1) * kB * kMaxN;
         const C v = row[t];
-        if (live) Fb[(size_t)t * nmax + r] = v;
-        T best = (live && !mine_used) ? abs2(v) : (T)-1;
-        int bi = (live && !mine_used) ? r : n;
+        if (live) {
+          Fb[(size_t)t * nmax + r] = v;
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-          const T ob = __shfl_down_sync(0xffffffffu, best, off);
-          const int oi = __shfl_down_sync(0xffffffffu, bi, off);
-          if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+          for (int q = 0; q < kB; ++q)
+            if (q < bt) RB[(size_t)q * kMaxN + r] = row[q];
         }
-        if (lane == 0) { wbest[warp] = best; wbi[warp] = bi; }
+        unsigned key = 0u;
+        if (live && !mine_used)
+          key = (__float_as_uint((float)abs2(v)) & 0xffffff00u) | (unsigned)(255 - r);
+        key = __reduce_max_sync(0xffffffffu, key);
+        unsigned* wk = wkey + (t & 1) * 8;   // by step parity, like RowB
+        if (lane == 0) wk[warp] = key;
         named_sync(1, kMaxN);
-        best = wbest[0];
-        bi = wbi[0];
+        unsigned best = wk[0];
 #pragma unroll
-        for (int w = 1; w < kMaxN / 32; ++w) {
-          const T ob = wbest[w];
-          const int oi = wbi[w];
-          if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-        }
-        if (!(best > (T)0) || !isfinite(best) || bi >= n) {
-          if (r == 0) atomicOr(status, 1);
-          // keep going with the first unpivoted row so the kernel terminates normally
-          bi = 0;
-          while (bi < n && used[bi]) ++bi;
-          if (bi >= n) bi = 0;
-        }
-        const int p = bi;
+        for (int w = 1; w < kMaxN / 32; ++w) best = max(best, wk[w]);
+        // best < 256: no unpivoted row with a positive magnitude (singular);
+        // the step still runs (on the lowest unpivoted row) so that the kernel
+        // terminates normally, and the status says the factor is invalid
+        if (best < 256u && r == 0) atomicOr(status, 1);
+        const int p = best ? 255 - (int)(best & 0xffu) : 0;
+        const C pv = RB[(size_t)t * kMaxN + p];
+        if (r == 0 && !isfinite((double)abs2(pv))) atomicOr(status, 1);
+        const C inv = crcp(pv);
         if (r == p) {
-          const C inv = crcp(v);
           mine_used = true;
           used[r] = 1;
           piv[k0 + t] = r;
           pbb[t] = r;
           ivb[t] = inv;
 #pragma unroll
-          for (int q = 0; q < kB; ++q) {
-            if (q < bt) {
-              row[q] = (q == t) ? inv : cmul(row[q], inv);
-              rowp[q] = row[q];
-            }
-          }
-        }
-        named_sync(1, kMaxN);
-        if (live && r != p) {
-          const C inv = ivb[t];
+          for (int q = 0; q < kB; ++q)
+            if (q < bt) row[q] = (q == t) ? inv : cmul(row[q], inv);
+        } else if (live) {
 #pragma unroll
           for (int q = 0; q < kB; ++q) {
             if (q < bt) {
               if (q == t) row[q] = cneg(cmul(v, inv));
-              else cfms(row[q], v, rowp[q]);
+              else cfms(row[q], v, cmul(RB[(size_t)q * kMaxN + p], inv));
             }
           }
         }
@@ -423,8 +433,14 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
         for (int s2 = t + 1; s2 < bt; ++s2) cfms(a, Fb[(size_t)s2 * nmax + pt], U[(size_t)s2 * ldw + cc]);
         W[(size_t)pt * ldw + cc] = a;
       }
-      if (na > 0) rank_update<T, NTHR>(Fb, U, W, pslot, n, nmax, ldw, bt, cb, xa, lt);
-      if (ce > xb) rank_update<T, NTHR>(Fb, U, W, pslot, n, nmax, ldw, bt, xb, ce, lt);
+      // per contiguous range; one column per thread where it is at most kTX wide
+      auto update = [&](int a0, int a1) {
+        if (a1 - a0 <= 0) return;
+        if (a1 - a0 <= kTX) rank_update<T, NTHR, 1>(Fb, U, W, pslot, n, nmax, ldw, bt, a0, a1, lt);
+        else rank_update<T, NTHR, CJ>(Fb, U, W, pslot, n, nmax, ldw, bt, a0, a1, lt);
+      };
+      update(cb, xa);
+      update(xb, ce);
     };
     using AllThreads = std::integral_constant<int, kFT>;
     using RestThreads = std::integral_constant<int, kFT - kMaxN>;
@@ -482,19 +498,23 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
         }
         __syncthreads();
       }
-      const bool look = more && (int)g == o2;
+      // the owner of the next block factors its panel: with look-ahead on its
+      // panel warps while its other warps finish the current block, otherwise
+      // after the whole update
+      const bool own_next = more && (int)g == o2;
+      const bool overlap = own_next && cur && lookahead != 0;
       const int pk0 = (cur && (int)g == o) ? k0 - c0 : -1;   // my panel columns [pk0, pk0 + bt), if any
       const int n0 = k1 - c0, n1 = k2 - c0;                  // the next panel's columns, if mine
-      if (cur && look) {
+      if (overlap) {
         finish(AllThreads{}, bt, buf, n0, n1, -1, -1);
         __syncthreads();
       }
-      if (look && tid < kMaxN) {
-        panel(k1, k2, (blk + 1) & 1);
-      } else if (cur) {
-        if (look) finish(RestThreads{}, bt, buf, 0, nc, pk0 >= 0 ? pk0 : n0, n1);
+      if (cur && !(overlap && tid < kMaxN)) {
+        if (overlap) finish(RestThreads{}, bt, buf, 0, nc, pk0 >= 0 ? pk0 : n0, n1);
         else finish(AllThreads{}, bt, buf, 0, nc, pk0, pk0 >= 0 ? pk0 + bt : -1);
       }
+      if (cur && !overlap) __syncthreads();
+      if (own_next && tid < kMaxN) panel(k1, k2, (blk + 1) & 1);
       __syncthreads();
       if (cur) {
         if (tid < bt) pslot[pbb[tid]] = -1;
@@ -529,8 +549,9 @@ template <typename T>
 size_t fac_smem(int nmax, int ldw) {
   using C = cx_t<T>;
   constexpr int kB = FacCfg<T>::B;
-  return 256 + 3 * (size_t)kMaxN * sizeof(int) + 2 * kB * sizeof(int) + (3 * kB + kB * kB) * sizeof(C) +
-         2 * (size_t)kB * nmax * sizeof(C) + (size_t)kB * ldw * sizeof(C) + (size_t)nmax * ldw * sizeof(C);
+  return 256 + 3 * (size_t)kMaxN * sizeof(int) + 2 * kB * sizeof(int) + (2 * kB + kB * kB) * sizeof(C) +
+         2 * (size_t)kB * nmax * sizeof(C) + (size_t)kB * ldw * sizeof(C) + (size_t)nmax * ldw * sizeof(C) +
+         2 * (size_t)kB * kMaxN * sizeof(C);
 }
 
 // smallest cluster whose column slices fit the update tiles and shared memory
@@ -561,7 +582,7 @@ size_t factor_smem_bytes(int ny, bool dbl) {
 template <typename T>
 cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* prof, const double* mgrid,
                              int n_dof, double omega2, void* fac, void* prev, int max_ny, int* status,
-                             cudaStream_t st, bool split) {
+                             cudaStream_t st, bool split, bool lookahead) {
   if (ncell <= 0) return cudaSuccess;
   if (max_ny > kMaxN) return cudaErrorInvalidValue;
   int dev = 0, maxopt = 0, ldw = 0;
@@ -595,7 +616,7 @@ cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* pro
     cfg.gridDim = dim3((unsigned)(ncell * G * (middle ? 1 : 2)));
     e = cudaLaunchKernelEx(&cfg, kern, cells, prof, mgrid, n_dof, omega2, reinterpret_cast<cx_t<T>*>(fac),
                            reinterpret_cast<cx_t<T>*>(split ? prev : nullptr), prev_stride, split ? 1 : 0, middle,
-                           G, max_ny, ldw, status);
+                           lookahead ? 1 : 0, G, max_ny, ldw, status);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -603,8 +624,8 @@ cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* pro
 
 
 template cudaError_t launch_factorize<float>(const DevCell*, int, const double2*, const double*, int, double,
-                                             void*, void*, int, int*, cudaStream_t, bool);
+                                             void*, void*, int, int*, cudaStream_t, bool, bool);
 template cudaError_t launch_factorize<double>(const DevCell*, int, const double2*, const double*, int, double,
-                                              void*, void*, int, int*, cudaStream_t, bool);
+                                              void*, void*, int, int*, cudaStream_t, bool, bool);
 
 }  // namespace lsw
