@@ -731,7 +731,9 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
         const int c0 = c * CW;
         const int ncol = min(CW, nJ - c0);
         if (ok && rows_ok) {
-  #pragma unroll 2
+          // deeper unrolling (more loads in flight) where the registers allow
+          constexpr int UNR = (R <= 4 && sizeof(T) == 4) ? 4 : 2;
+  #pragma unroll UNR
           for (int cc = ks; cc < ncol; cc += KSW) {
             Pair<T> s;
             s.load(S + (size_t)cc * ldn);
