@@ -376,7 +376,7 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
         if (best < 256u && r == 0) atomicOr(status, 1);
         const int p = best ? 255 - (int)(best & 0xffu) : 0;
         const C pv = RB[(size_t)t * kMaxN + p];
-        if (r == 0 && !isfinite((double)abs2(pv))) atomicOr(status, 1);
+        if (r == 0 && !isfinite(abs2(pv))) atomicOr(status, 1);   // in T: FP64 is slow on this part
         const C inv = crcp(pv);
         if (r == p) {
           mine_used = true;
