@@ -13,7 +13,11 @@ precision.
   request with the same key reuses the factors.  Device memory is the
   admission budget: a request whose operator is not resident is admitted when
   its estimated footprint fits after evicting idle operators (least recently
-  used first); otherwise it waits until running work frees memory.
+  used first); otherwise it waits until running work frees memory.  An
+  operator with no request waiting returns its solve workspace (Krylov bases,
+  sweep pools) when its batch ends and is charged only its factors while
+  idle; its next batch is admitted for the growth back to the batch
+  footprint, so far more operators stay resident than their peak sizes allow.
 * Continuous batching: every slot (a host thread with its own CUDA stream)
   takes the oldest admissible request and every other waiting request for
   the same operator (up to ``max_batch``), and solves them as one
@@ -164,6 +168,12 @@ class GpuOperator:
             r.iterations = rep.iterations
             r.true_rel_res = float(resh[i])
 
+    def release(self) -> int:
+        """Return the Krylov bases and sweep pools to the device (the factors
+        stay); the bytes the operator still holds."""
+        self.solver.release_workspace()
+        return int(self.solver.info()["device_bytes"])
+
     def close(self) -> None:
         self.solver.close()
 
@@ -211,20 +221,20 @@ class FactorCache:
     def used(self) -> int:
         return sum(e.bytes for e in self.entries.values())
 
-    def can_admit(self, nbytes: int) -> bool:
-        """Whether `nbytes` fit after evicting every idle entry."""
-        idle = sum(e.bytes for e in self.entries.values() if not e.busy)
+    def can_admit(self, nbytes: int, keep=None) -> bool:
+        """Whether `nbytes` fit after evicting every idle entry but `keep`."""
+        idle = sum(e.bytes for e in self.entries.values() if not e.busy and e is not keep)
         return self.used - idle + nbytes <= self.budget
 
-    def make_room(self, nbytes: int) -> list:
-        """Evict idle entries (LRU first) until `nbytes` fit; returns the
-        evicted entries (their operators still have to be closed)."""
+    def make_room(self, nbytes: int, keep=None) -> list:
+        """Evict idle entries but `keep` (LRU first) until `nbytes` fit; returns
+        the evicted entries (their operators still have to be closed)."""
         out = []
         for k in sorted(self.entries, key=lambda k: self.entries[k].last_used):
             if self.used + nbytes <= self.budget:
                 break
             e = self.entries[k]
-            if e.busy:
+            if e.busy or e is keep:
                 continue
             del self.entries[k]
             out.append(e)
@@ -309,6 +319,17 @@ class ServeEngine:
             if e is not None:
                 if e.busy:
                     continue
+                # an idle operator that returned its workspace grows back to
+                # the batch footprint: admit the growth like a new operator
+                need = estimate_bytes(r.spec, r.precision, self.max_batch, self.restart)
+                grow = need - e.bytes
+                if grow > 0:
+                    if not self.cache.can_admit(grow, keep=e):
+                        continue
+                    for ev in self.cache.make_room(grow, keep=e):
+                        if ev.op is not None:
+                            ev.op.close()
+                    e.bytes = need
                 hit = True
             else:
                 need = estimate_bytes(r.spec, r.precision, self.max_batch, self.restart)
@@ -361,6 +382,17 @@ class ServeEngine:
             except Exception as ex:  # a failed solve fails its requests, not the loop
                 err = f"{type(ex).__name__}: {ex}"
             t_done = self.clock() - self._t0
+            # nothing waiting for this operator: it returns its solve workspace
+            # (outside the lock: freeing device memory waits for the device) and
+            # is charged only the bytes it keeps while idle
+            resident = None
+            with self._cv:
+                idle_next = err is None and not any(q.key() == e.key for q in self._pending)
+            if idle_next and e.op is not None and hasattr(e.op, "release"):
+                try:
+                    resident = int(e.op.release())
+                except Exception:
+                    resident = None
             with self._cv:
                 for r in batch:
                     r.t_done = t_done
@@ -368,6 +400,8 @@ class ServeEngine:
                     self._done.append(r)
                 if e.op is not None:
                     e.bytes = max(e.bytes, int(getattr(e.op, "bytes", e.bytes)))
+                if resident is not None:
+                    e.bytes = resident
                 if err is not None and not e.ready:
                     self.cache.entries.pop(e.key, None)
                     if e.op is not None:

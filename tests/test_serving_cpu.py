@@ -103,6 +103,34 @@ def test_budget_evicts_least_recently_used_idle_operator():
     assert set(eng.cache.entries) == {seq[0].key(), seq[3].key()}
 
 
+class ReleasingOp(FakeOp):
+    """A fake operator that keeps only a small resident part when idle."""
+
+    def release(self):
+        self.log.append(("release", self.key))
+        return 10
+
+
+class ReleasingBackend(FakeBackend):
+    def create(self, req, stream):
+        return ReleasingOp(req, self.log, self.factor_s)
+
+
+def test_idle_operators_return_their_workspace_and_stay_resident():
+    be = ReleasingBackend()
+    b1 = one_op_bytes()
+    # the budget of the eviction test above: without the release one operator
+    # had to go, with it all three stay and the repeat is a cache hit
+    eng = ServeEngine(be, slots=1, max_batch=4, budget=2 * b1 + 10)
+    seq = [_req(0, 0, 0.00), _req(1, 1, 0.05), _req(2, 2, 0.10), _req(3, 1, 0.15)]
+    st = eng.run(seq, realtime=True)
+    assert st.n == 4 and st.failures == 0
+    assert st.evictions == 0 and st.factorisations == 3 and st.cache_hits == 1
+    assert len([e for e in be.log if e[0] == "release"]) == 4
+    # idle entries are charged their resident bytes
+    assert all(e.bytes == 10 for e in eng.cache.entries.values())
+
+
 def test_busy_operator_is_never_evicted():
     c = FactorCache(budget=100)
     from lsweeps.serving import CacheEntry, OperatorKey
