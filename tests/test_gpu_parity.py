@@ -101,6 +101,21 @@ def test_fgmres_solves_to_tolerance(f, prec):
     assert rel(x.cpu().numpy(), d["x_direct"]) <= 1e-5
 
 
+def test_one_cell_precond_is_the_exact_inverse():
+    """N = 1: the only cell is the whole domain, so the L-sweep preconditioner
+    is A^-1 (the other three shifted windows are empty); FGMRES then converges
+    in one iteration."""
+    spec, med = small(N=1, m=30, p=6, medium="lens")
+    S = _solver(spec, med, "c128")
+    rng = np.random.default_rng(17)
+    v = rng.standard_normal(S.n2) + 1j * rng.standard_normal(S.n2)
+    y = S.apply_precond(_dev(v))
+    assert rel(S.apply_A(y).cpu().numpy(), v) <= 1e-10
+    b = S.assemble_rhs(spec.sources)
+    x, rep = S.gmres(b, mode="flexible", tol=1e-8, max_iter=10, restart=10)
+    assert rep.iterations <= 1 and rep.true_rel_res <= 1e-8
+
+
 def test_batched_rhs_equal_single():
     """A batch of right-hand sides gives each one's single result; only the
     summation order inside a cell solve may differ (the number of consumer
