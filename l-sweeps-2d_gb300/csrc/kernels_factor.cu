@@ -136,13 +136,14 @@ __device__ __forceinline__ uint2 split_entry(float2 v) {
 // block-column owner: CTA g owns the columns [g n/G, (g+1) n/G)
 __device__ __forceinline__ int col_owner(int j, int n, int G) { return ((j + 1) * G - 1) / n; }
 
-// Rank-bt update of the non-pivot rows on columns [cb, ce) of W:
-// c[r] -= sum_t f_t[r] u_t, register-tiled (kRI rows x CJ columns per thread,
-// kTX x CJ columns per pass) over NTHR threads; lt = thread index within them.
+// Rank-bt update of the non-pivot rows on columns [cb, ce) of W except
+// [x0, x1) (computed in the tiles, not stored): c[r] -= sum_t f_t[r] u_t,
+// register-tiled (kRI rows x CJ columns per thread, kTX x CJ columns per pass)
+// over NTHR threads; lt = thread index within them.
 template <typename T, int NTHR, int CJ>
 __device__ __forceinline__ void rank_update_body(const cx_t<T>* __restrict__ Fb, const cx_t<T>* __restrict__ U,
                                             cx_t<T>* __restrict__ W, const int* __restrict__ pslot, int n,
-                                            int nmax, int ldw, int bt, int cb, int ce, int lt) {
+                                            int nmax, int ldw, int bt, int cb, int ce, int x0, int x1, int lt) {
   using C = cx_t<T>;
   constexpr int NTY = NTHR / kTX;
   const C z = czero<C>();
@@ -177,7 +178,7 @@ __device__ __forceinline__ void rank_update_body(const cx_t<T>* __restrict__ Fb,
 #pragma unroll
       for (int b = 0; b < CJ; ++b) {
         const int cc = cb + tx + kTX * b;
-        if (cc >= ce) continue;
+        if (cc >= ce || (cc >= x0 && cc < x1)) continue;
         C* w = W + (size_t)r * ldw + cc;
         *w = csub(*w, acc[a][b]);
       }
@@ -190,15 +191,16 @@ __device__ __forceinline__ void rank_update_body(const cx_t<T>* __restrict__ Fb,
 template <typename T, int NTHR, int CJ>
 __device__ __noinline__ void rank_update_call(const cx_t<T>* __restrict__ Fb, const cx_t<T>* __restrict__ U,
                                                  cx_t<T>* __restrict__ W, const int* __restrict__ pslot, int n,
-                                                 int nmax, int ldw, int bt, int cb, int ce, int lt) {
-  rank_update_body<T, NTHR, CJ>(Fb, U, W, pslot, n, nmax, ldw, bt, cb, ce, lt);
+                                                 int nmax, int ldw, int bt, int cb, int ce, int x0, int x1,
+                                                 int lt) {
+  rank_update_body<T, NTHR, CJ>(Fb, U, W, pslot, n, nmax, ldw, bt, cb, ce, x0, x1, lt);
 }
 template <typename T, int NTHR, int CJ>
 __device__ __forceinline__ void rank_update(const cx_t<T>* __restrict__ Fb, const cx_t<T>* __restrict__ U,
                                             cx_t<T>* __restrict__ W, const int* __restrict__ pslot, int n,
-                                            int nmax, int ldw, int bt, int cb, int ce, int lt) {
-  if constexpr (sizeof(T) == 4) rank_update_call<T, NTHR, CJ>(Fb, U, W, pslot, n, nmax, ldw, bt, cb, ce, lt);
-  else rank_update_body<T, NTHR, CJ>(Fb, U, W, pslot, n, nmax, ldw, bt, cb, ce, lt);
+                                            int nmax, int ldw, int bt, int cb, int ce, int x0, int x1, int lt) {
+  if constexpr (sizeof(T) == 4) rank_update_call<T, NTHR, CJ>(Fb, U, W, pslot, n, nmax, ldw, bt, cb, ce, x0, x1, lt);
+  else rank_update_body<T, NTHR, CJ>(Fb, U, W, pslot, n, nmax, ldw, bt, cb, ce, x0, x1, lt);
 }
 
 template <typename T>
@@ -433,14 +435,13 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
         for (int s2 = t + 1; s2 < bt; ++s2) cfms(a, Fb[(size_t)s2 * nmax + pt], U[(size_t)s2 * ldw + cc]);
         W[(size_t)pt * ldw + cc] = a;
       }
-      // per contiguous range; one column per thread where it is at most kTX wide
-      auto update = [&](int a0, int a1) {
-        if (a1 - a0 <= 0) return;
-        if (a1 - a0 <= kTX) rank_update<T, NTHR, 1>(Fb, U, W, pslot, n, nmax, ldw, bt, a0, a1, lt);
-        else rank_update<T, NTHR, CJ>(Fb, U, W, pslot, n, nmax, ldw, bt, a0, a1, lt);
-      };
-      update(cb, xa);
-      update(xb, ce);
+      // one tiled pass over [cb, ce) that stores nothing in [xa, xb) (their
+      // products use stale U and are dropped); one column per thread where
+      // the range is at most kTX wide
+      if (ncols > 0) {
+        if (ce - cb <= kTX) rank_update<T, NTHR, 1>(Fb, U, W, pslot, n, nmax, ldw, bt, cb, ce, xa, xb, lt);
+        else rank_update<T, NTHR, CJ>(Fb, U, W, pslot, n, nmax, ldw, bt, cb, ce, xa, xb, lt);
+      }
     };
     using AllThreads = std::integral_constant<int, kFT>;
     using RestThreads = std::integral_constant<int, kFT - kMaxN>;
