@@ -40,8 +40,12 @@
 // warp 3 copies y_k (forward) and x_k (backward) to a per-item scratch; the
 // remaining warps are consumers: a lane owns a row pair of a 64-row group and
 // a warp one of KSW interleaved column slices, accumulating in registers with
-// no cross-lane reduction.  Line vectors and partial sums are stored
-// [column][slot] so that slot offsets are compile-time constants.  The
+// no cross-lane reduction (complex FP32/FP64 FMAs).  With split factors (bf16
+// hi + lo words) a consumer warp owns a 16-row m-tile instead and runs the
+// partial products on the tensor cores (mma.sync m16n8k16, three products per
+// k-step, FP32 accumulation) against the line input staged as bf16 hi/lo
+// words.  Line vectors and partial sums are stored [column][slot] so that
+// slot offsets are compile-time constants.  The
 // outputs (owned DOFs, trace lines, cell vectors) are written once per item
 // from the scratch by every non-producer thread after the backward pass, each
 // half writing its own lines.
