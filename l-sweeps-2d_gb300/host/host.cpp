@@ -244,10 +244,10 @@ void DDCheckerboard::setUp(const Assembler* assembler, const LocalLinearSolver* 
   if (domain.size() != 2 || nCells.size() != 2 || nElsInCell.size() != 2)
     throw lsw_host_error("ERROR: DDCheckerboard is two-dimensional");
   if (nCells[0] != nCells[1] || nElsInCell[0] != nElsInCell[1])
-    throw lsw_host_error("ERROR: this build supports square checkerboards (NCellsX == NCellsY, NX == NY)");
+    throw lsw_host_error("ERROR: this library supports square checkerboards (NCellsX == NCellsY, NX == NY)");
   const double lx = domain[0][1] - domain[0][0], ly = domain[1][1] - domain[1][0];
-  if (!(lx > 0) || std::fabs(lx - ly) > 1e-12 * lx) throw lsw_host_error("ERROR: this build supports square domains");
-  if (assembler->getOrder() != 2) throw lsw_host_error("ERROR: this build supports Order = 2");
+  if (!(lx > 0) || std::fabs(lx - ly) > 1e-12 * lx) throw lsw_host_error("ERROR: this library supports square domains");
+  if (assembler->getOrder() != 2) throw lsw_host_error("ERROR: this library supports Order = 2");
   mDomain = domain;
   mN = (int)nCells[0];
   mM = (int)nElsInCell[0];

@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
 ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may import this
-module, and only as the checker or the timed CPU baseline.  The product path
+module, and only as the reference results or the timed CPU baseline.  The product path
 (the CUDA library behind ``include/lsweeps.h``) never calls it.
 
 Parity status: **parity unpinned by the reference.**  The reference ships no
