@@ -64,7 +64,10 @@ def _oracle_geometry(P, c_idx):
     return out
 
 
-@pytest.mark.parametrize("N,m,p", [(1, 6, 2), (2, 10, 4), (3, 12, 5), (4, 8, 3)])
+@pytest.mark.parametrize("N,m,p", [(1, 6, 2), (2, 10, 4), (3, 12, 5), (4, 8, 3),
+                                   # odd and even cell sizes, thin and thick PML, more cells,
+                                   # and the 192-DOF limit
+                                   (5, 7, 2), (6, 5, 1), (3, 31, 9), (8, 16, 6), (2, 149, 20)])
 def test_geometry_matches_oracle(N, m, p):
     spec, med = small(N=N, m=m, p=p)
     P = OracleProblem(spec.N, spec.m, spec.p, spec.h, spec.omega, med)
