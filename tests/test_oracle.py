@@ -24,26 +24,28 @@ def test_fd_weights_central():
     assert np.allclose(fd_weights(1, np.arange(3.0), 1), [-0.5, 0, 0.5])
 
 
-@pytest.mark.parametrize("N", [1, 2, 3])
-def test_ownership_partition(N):
-    _, _, P = _problem(N)
+@pytest.mark.parametrize("N,m,p", [(1, 10, 4), (2, 10, 4), (3, 10, 4), (4, 7, 2), (5, 6, 3)])
+def test_ownership_partition(N, m, p):
+    _, _, P = _problem(N, m=m, p=p)
     for key, keep in P.dd.keep.items():
         from oracle.lsweeps_oracle import global_indices
         g = np.concatenate(global_indices(P.dd, P.h, P.p, P.n_dof, *key))
         assert g.size == P.n_dof ** 2 and np.unique(g).size == g.size
 
 
-@pytest.mark.parametrize("N", [2, 3])
-def test_dd_matvec_equals_global_operator(N):
-    _, _, P = _problem(N)
+@pytest.mark.parametrize("N,m,p,medium", [(2, 10, 4, "lens"), (3, 10, 4, "lens"), (4, 7, 2, "layered"),
+                                          (3, 9, 5, "random")])
+def test_dd_matvec_equals_global_operator(N, m, p, medium):
+    _, _, P = _problem(N, m=m, p=p, medium=medium)
     A = P.global_matrix()
     rng = np.random.default_rng(0)
     v = rng.standard_normal(P.n_dof ** 2) + 1j * rng.standard_normal(P.n_dof ** 2)
     assert np.linalg.norm(P.apply_A_global(v) - A @ v) <= 1e-14 * np.linalg.norm(A @ v)
 
 
-def test_windows_partition():
-    _, _, P = _problem(3)
+@pytest.mark.parametrize("N,m,p", [(3, 10, 4), (2, 7, 2), (4, 6, 3)])
+def test_windows_partition(N, m, p):
+    _, _, P = _problem(N, m=m, p=p)
     rng = np.random.default_rng(1)
     x = P.C(rng.standard_normal(P.n_dof ** 2) + 0j)
     parts = [P.dd.get_separated_rhs(x, a, b) for a, b in ((0, 0), (1, 0), (0, 1), (1, 1))]
