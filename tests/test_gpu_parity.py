@@ -101,6 +101,23 @@ def test_fgmres_solves_to_tolerance(f, prec):
     assert rel(x.cpu().numpy(), d["x_direct"]) <= 1e-5
 
 
+@pytest.mark.parametrize("N,m,p,medium", [(5, 7, 2, "layered"), (2, 20, 8, "random"), (6, 5, 1, "lens")])
+def test_precond_more_geometries(N, m, p, medium):
+    """The preconditioner against the oracle on decompositions beyond the
+    fixtures: a thin PML, more cells, odd cell sizes, all three media."""
+    from oracle.lsweeps_oracle import OracleProblem
+    spec, med = small(N=N, m=m, p=p, medium=medium)
+    P = OracleProblem(spec.N, spec.m, spec.p, spec.h, spec.omega, med)
+    P.dd.factorize()
+    rng = np.random.default_rng(N * 100 + m)
+    v = rng.standard_normal(P.n_dof ** 2) + 1j * rng.standard_normal(P.n_dof ** 2)
+    y_or = P.apply_precond_global(v)
+    for prec, tol in (("c128", 1e-10), ("c64", 2e-4), ("bf16x2", 2e-4)):
+        S = _solver(spec, med, prec)
+        assert rel(S.apply_precond(_dev(v)).cpu().numpy(), y_or) <= tol, prec
+        S.close()
+
+
 def test_one_cell_precond_is_the_exact_inverse():
     """N = 1: the only cell is the whole domain, so the L-sweep preconditioner
     is A^-1 (the other three shifted windows are empty); FGMRES then converges
