@@ -144,6 +144,20 @@ def test_busy_operator_is_never_evicted():
     assert [e.key for e in ev] == [k2] and k1 in c.entries
 
 
+def test_regrowth_never_evicts_the_operator_itself():
+    c = FactorCache(budget=100)
+    from lsweeps.serving import CacheEntry, OperatorKey
+    k1 = OperatorKey(1, 1, 1, 1.0, 1.0, "a", "c64")
+    k2 = OperatorKey(1, 1, 1, 1.0, 1.0, "b", "c64")
+    e1 = CacheEntry(k1, 10, busy=False, last_used=0.0)     # released, about to regrow
+    e2 = CacheEntry(k2, 50, busy=False, last_used=1.0)
+    c.entries[k1], c.entries[k2] = e1, e2
+    assert not c.can_admit(95, keep=e1)     # 10 kept + 95 > 100 even with e2 evicted
+    assert c.can_admit(80, keep=e1)
+    ev = c.make_room(80, keep=e1)
+    assert [e.key for e in ev] == [k2] and k1 in c.entries
+
+
 def test_oversized_request_fails_and_loop_ends():
     be = FakeBackend()
     eng = ServeEngine(be, slots=2, max_batch=4, budget=one_op_bytes() // 2)
