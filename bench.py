@@ -121,6 +121,17 @@ def measured_peaks():
 # ---------------------------------------------------------------------------
 # CPU baseline: the oracle (SuperLU local solves) on a bounded sample
 # ---------------------------------------------------------------------------
+def max_over_ranks(x: float, dist=None, device="cpu") -> float:
+    """The maximum of x over the ranks of the process group (x itself without
+    one); the tensor lives on `device` (the GPU for NCCL, the CPU for gloo)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def _interior_cell(spec, med):
     """One interior C2-shaped cell (column/row 1: interior domain [a - 2h, b + 4h],
     (m + 6 + 2p - 1)^2 DOFs), assembled by the oracle."""
@@ -316,11 +327,7 @@ def run_gpu(args):
         dist.barrier()
     gpu_launches = S.info()["kernel_launches"] - launches0
     step_ms = [a.elapsed_time(c) for a, c in ev]
-    dev_total = sum(step_ms) / 1e3
-    if dist:
-        t = torch.tensor([dev_total], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_total = float(t.item())
+    dev_total = max_over_ranks(sum(step_ms) / 1e3, dist, dev)
     value = world * args.steps * nrhs / dev_total   # right-hand sides solved per second
 
     # end to end through the host-buffer C call (H2D of b, D2H of x in the timed region)
