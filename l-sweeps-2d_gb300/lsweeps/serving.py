@@ -261,6 +261,7 @@ class ServeStats:
     mean_batch: float
     max_in_flight: int
     failures: int
+    oom_retries: int = 0
 
     def as_dict(self) -> dict:
         return dict(self.__dict__)
@@ -298,6 +299,7 @@ class ServeEngine:
         self._batched = 0
         self._hits = 0
         self._factorisations = 0
+        self._oom_retries = 0
         self._t0 = 0.0
 
     # -- scheduling (called with the lock held) --------------------------------
@@ -350,6 +352,25 @@ class ServeEngine:
             return e, batch
         return None
 
+    def _oom_retry(self, e, fn):
+        """Run fn; if the device ran out of memory (the footprint estimate was
+        low), evict every idle operator but e and run it once more."""
+        try:
+            return fn()
+        except Exception as ex:
+            if "OUT_OF_MEMORY" not in str(ex) and "out of memory" not in str(ex).lower():
+                raise
+            with self._cv:
+                victims = [x for x in self.cache.entries.values() if not x.busy and x is not e]
+                for v in victims:
+                    del self.cache.entries[v.key]
+                    self.cache.evictions += 1
+                self._oom_retries += 1
+            for v in victims:
+                if v.op is not None:
+                    v.op.close()
+            return fn()
+
     def _worker(self, slot: int):
         stream = self.backend.new_stream()
         while True:
@@ -373,12 +394,12 @@ class ServeEngine:
             err = None
             try:
                 if e.op is None:
-                    e.op = self.backend.create(batch[0], stream)
+                    e.op = self._oom_retry(e, lambda: self.backend.create(batch[0], stream))
                     self._factorisations += 1
                     e.ready = True
                 else:
                     self._hits += len(batch)
-                e.op.solve(batch, stream, restart=self.restart)
+                self._oom_retry(e, lambda: e.op.solve(batch, stream, restart=self.restart))
             except Exception as ex:  # a failed solve fails its requests, not the loop
                 err = f"{type(ex).__name__}: {ex}"
             t_done = self.clock() - self._t0
@@ -453,7 +474,8 @@ class ServeEngine:
             wait_p50_ms=_pct(waits, 0.5), cache_hits=self._hits, factorisations=self._factorisations,
             evictions=self.cache.evictions - getattr(self, "_evictions0", 0), batches=self._batches,
             mean_batch=self._batched / self._batches if self._batches else 0.0,
-            max_in_flight=self._max_in_flight, failures=len(self._done) - len(done))
+            max_in_flight=self._max_in_flight, failures=len(self._done) - len(done),
+            oom_retries=self._oom_retries)
 
     def close(self) -> None:
         for e in list(self.cache.entries.values()):

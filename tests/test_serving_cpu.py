@@ -131,6 +131,35 @@ def test_idle_operators_return_their_workspace_and_stay_resident():
     assert all(e.bytes == 10 for e in eng.cache.entries.values())
 
 
+class OomOnceOp(FakeOp):
+    """Fails its first solve as the device would when memory runs out."""
+    tripped = False
+
+    def solve(self, reqs, stream, restart=30):
+        if not OomOnceOp.tripped:
+            OomOnceOp.tripped = True
+            raise RuntimeError("LSW_ERR_OUT_OF_MEMORY: cudaMalloc(Z): out of memory")
+        super().solve(reqs, stream, restart)
+
+
+class OomOnceBackend(FakeBackend):
+    def create(self, req, stream):
+        if req.rid == 2:
+            return OomOnceOp(req, self.log, self.factor_s)
+        return FakeOp(req, self.log, self.factor_s)
+
+
+def test_out_of_memory_evicts_idle_operators_and_retries():
+    be = OomOnceBackend()
+    eng = ServeEngine(be, slots=1, max_batch=4, budget=10 * one_op_bytes())
+    seq = [_req(0, 0, 0.00), _req(1, 1, 0.05), _req(2, 2, 0.10)]
+    st = eng.run(seq, realtime=True)
+    assert st.n == 3 and st.failures == 0 and st.oom_retries == 1
+    # the two idle operators were evicted to make room for the retry
+    assert st.evictions == 2 and {e[1] for e in be.log if e[0] == "close"} >= {seq[0].key(), seq[1].key()}
+    assert seq[2].x is not None
+
+
 def test_busy_operator_is_never_evicted():
     c = FactorCache(budget=100)
     from lsweeps.serving import CacheEntry, OperatorKey
