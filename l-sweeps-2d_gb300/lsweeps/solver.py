@@ -37,7 +37,13 @@ class SolveReport:
 
 
 class Solver:
-    """DDCheckerboard + LocalLinearSolverCUDA + GlobalIterativeSolverGMRES on one GPU."""
+    """DDCheckerboard + LocalLinearSolverCUDA + GlobalIterativeSolverGMRES on one GPU.
+
+    precision: "c128" / "fp64" (complex double factors and sweeps, the
+    reference's arithmetic), "c64" / "mixed" (complex float, FP32 accumulation)
+    or "bf16x2" / "split" (factor entries as bf16 hi + lo terms, tensor-core
+    products, FP32 accumulation); the Krylov solver is FP64 in every case.
+    """
 
     def __init__(self, spec: ProblemSpec, m_grid: np.ndarray, precision: str = "c64", device: int = 0):
         torch = _torch()
