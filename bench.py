@@ -1,9 +1,12 @@
 """Benchmark of the GB300 L-sweeps path: FGMRES + checkerboard L-sweep
-preconditioner solves of configuration C2 (1031^2 elements, Gaussian-lens
-medium, 8 x 8 cells of 128^2, PML 16, 8 points per wavelength at c_min).
+preconditioner solves.  Default workload C4: 4127^2 elements, seeded
+piecewise-smooth medium c in [1.5, 5.0], 32 x 32 cells of 128^2, PML 20,
+8 points per wavelength at c_min, one centred source; `--config C1..C3`
+selects the other workloads.
 
 A step is one complete solve to true relative residual 1e-6 with the cell
-factors resident in HBM (complex64 factors and applies inside FP64 flexible
+factors resident in HBM (the workload's factor arithmetic -- BF16-split
+tensor-core products for C4, complex64 for C1-C3 -- inside FP64 flexible
 GMRES(30)); the plain FP64 GPU path (complex128 factors) is measured beside it.
 Prints one JSON line (see the keys below).  `--impl reference` times the CPU
 oracle's restatement of the reference instead (the reference itself cannot be
@@ -39,7 +42,7 @@ WORKLOADS = {
     "C4": "C4: 2D Helmholtz, 4127^2 elements, seeded piecewise-smooth c in [1.5,5.0] (sigma 8 cells), "
           "8 ppw at c_min, 32x32 checkerboard of 128^2 cells, PML 20, 1 centred source, FGMRES(30) tol 1e-6",
 }
-WORKLOAD = WORKLOADS["C2"]
+WORKLOAD = WORKLOADS["C4"]
 # factor and sweep arithmetic per workload: complex FP32 where the workload names it, the
 # BF16-split tensor-core products (hi + lo bf16 terms, FP32 accumulation) for the 4096^2 case
 PRECISION = {"C1": "c64", "C2": "c64", "C3": "c64", "C4": "bf16x2"}
@@ -378,7 +381,8 @@ def run_gpu(args):
         torch.cuda.synchronize()
         f64_fact = e0.elapsed_time(e1) / 1e3
         x64 = torch.empty_like(b)
-        S64.gmres(b, mode="flexible", tol=args.tol, max_iter=300, restart=30, x=x64)
+        if args.fp64_warmup:
+            S64.gmres(b, mode="flexible", tol=args.tol, max_iter=300, restart=30, x=x64)
         t64, r64 = [], None
         for _ in range(args.fp64_steps):
             a1, a2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -388,7 +392,13 @@ def run_gpu(args):
             torch.cuda.synchronize()
             t64.append(a1.elapsed_time(a2))
         fp64 = {"p50_ms": pctl(t64, 0.5), "p99_ms": pctl(t64, 0.99), "iterations": r64.iterations,
-                "true_rel_res": r64.true_rel_res, "factorize_s": f64_fact, "steps": len(t64)}
+                "true_rel_res": r64.true_rel_res, "factorize_s": f64_fact, "steps": len(t64),
+                "warmup_solves": args.fp64_warmup}
+        # the mixed and FP64 solutions of the same right-hand side agree
+        fp64["rel_diff_vs_mixed"] = float((x - x64).norm() / x64.norm())
+        S64.close()
+        S64 = None
+        torch.cuda.empty_cache()
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -487,7 +497,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--tol", type=float, default=1e-6)
-    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--fp64-warmup", type=int, default=None,
+                    help="untimed FP64 solves before the timed ones (default 1, 0 for C4: ~85 s each)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--ref-budget", type=float, default=15.0)
@@ -499,11 +511,13 @@ def main():
     ap.add_argument("--serve-rates", default="1,4,16")
     ap.add_argument("--serve-requests", type=int, default=40)
     ap.add_argument("--serve-slots", type=int, default=4)
-    ap.add_argument("--config", default="C2")
+    ap.add_argument("--config", default="C4")
     ap.add_argument("--precision", default=None, choices=["c64", "bf16x2", "c128"],
                     help="factor/sweep arithmetic (default: the workload's, c64 for C1-C3, bf16x2 for C4)")
     ap.add_argument("--nrhs", type=int, default=1)
     args = ap.parse_args()
+    if args.fp64_warmup is None:
+        args.fp64_warmup = 0 if args.config.upper() == "C4" else 1
     if args.serve:
         run_serve(args)
         return

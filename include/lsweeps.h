@@ -149,6 +149,19 @@ lsw_status lsw_ctx_destroy(lsw_ctx* ctx);
 const char* lsw_status_string(lsw_status s);
 const char* lsw_ctx_last_error(const lsw_ctx* ctx);
 
+/* Limit of every bounded wait inside the context's kernels (default ~2 s).
+ * A wait that runs out makes its kernel give up and return normally; the call
+ * that launched it then returns LSW_ERR_CUDA (results invalid).  No
+ * counterpart in the reference (its blocking MPI_Recv waits without limit,
+ * DDCheckerboard.cpp:976-1164). */
+lsw_status lsw_ctx_set_wait_limit(lsw_ctx* ctx, double seconds);
+
+/* Runs one bounded wait of the kernels' kind on a barrier that nothing
+ * completes, with the context's limit: returns LSW_ERR_CUDA once the limit
+ * has run out, and the context stays usable.  A check of the failure path for
+ * deployments; no counterpart in the reference. */
+lsw_status lsw_selftest_bounded_wait(lsw_ctx* ctx, void* stream);
+
 /* Geometry of cell `cell` (index I*N + J) of a decomposition, computed on the
  * host without a GPU (DDCheckerboard::setUp trace limits, DDCheckerboard.cpp:214-419,
  * and SubdomainStructured::assignIndexSets, SubdomainStructured.cpp:1019-1116). */
@@ -170,7 +183,9 @@ lsw_status lsw_cell_info_get(const lsw_ctx* ctx, int cell, lsw_cell_info* out);
 lsw_status lsw_factorize(lsw_ctx* ctx, void* stream);
 
 /* DDCheckerboard::applyPrecond (DDCheckerboard.cpp:687-739): y = M^-1 x for a
- * batch of nrhs global vectors. */
+ * batch of nrhs global vectors.  Asynchronous: it returns launch errors only;
+ * a kernel that gave up on a bounded wait is reported (once) by the next call
+ * that synchronises (lsw_apply_precond_profiled, lsw_gmres, lsw_local_solve). */
 lsw_status lsw_apply_precond(lsw_ctx* ctx, const void* x_dev, void* y_dev, int nrhs, void* stream);
 
 /* lsw_apply_precond with the front kernels timed by CUDA events; synchronises
@@ -228,8 +243,8 @@ lsw_status lsw_local_solve(lsw_ctx* ctx, int cell, const void* b_dev, void* x_de
  * 8 MiB device array inside the library, which every GPU that loads the
  * library holds until the process exits; a request that does not fit returns
  * LSW_ERR_INVALID_ARGUMENT with the sizes in lsw_ctx_last_error.
- * The first call on a device looks up that array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * lsw_ctx_create looks up that array's device address once, on the context's
+ * device, and keeps it with the context.
  * All calls share the array: calls that overlap on the GPU (other streams,
  * other contexts on the same device) race and must be serialised by the
  * caller.  Nothing in the array needs clearing between calls: every element

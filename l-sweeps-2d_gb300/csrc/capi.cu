@@ -71,6 +71,11 @@ struct lsw_ctx {
   int max_cluster = 8;
   int krylov_batch = 0;   // right-hand sides per Krylov sub-batch at most (0: as memory allows)
   bool factor_lookahead = true;
+  // bounded-wait limit of the sweep and factorisation kernels, in SM clock cycles
+  long long wait_cycles = 4000000000LL;   // ~2 s at 2 GHz
+  // device address of the allocation-free solve's fixed scratch array on this
+  // context's device (looked up once, with the device current, at creation)
+  void* noalloc_base = nullptr;
   // optional per-front timing of one apply
   std::vector<cudaEvent_t>* front_events = nullptr;
 };
@@ -231,6 +236,7 @@ lsw_status precond_impl(lsw_ctx* ctx, const double2* x, double2* y, int nrhs, cu
   a.x_stride = ctx->n2;
   a.n_dof = ctx->n_dof; a.N = ctx->N; a.m = ctx->m; a.p = ctx->p;
   a.err = ctx->d_status.as<int>() + 1;
+  a.wait_cycles = ctx->wait_cycles;
   a.split = ctx->prec == LSW_PREC_SPLIT ? 1 : 0;
   for (size_t fi = 0; fi < sc->fronts.size(); ++fi) {
     const Front& f = sc->fronts[fi];
@@ -259,11 +265,15 @@ lsw_status apply_A_impl(lsw_ctx* ctx, const double2* x, double2* y, int nrhs, cu
   return LSW_OK;
 }
 
-// reads the sweep kernels' error word (synchronises the stream)
+// Reads the sweep kernels' error word (synchronises the stream).  A set word
+// is cleared once it is reported, so an error raised by an asynchronous call
+// (lsw_apply_precond) is reported by the next call that checks, and later
+// calls that succeed report success.
 lsw_status check_kernel_err(lsw_ctx* ctx, cudaStream_t st) {
   int e = 0;
   CK(cudaMemcpyAsync(&e, ctx->d_status.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H err");
   CK(cudaStreamSynchronize(st), "sync");
+  if (e) CK(cudaMemsetAsync(ctx->d_status.as<int>() + 1, 0, sizeof(int), st), "clear err");
   if (e & 4) return fail(ctx, LSW_ERR_CUDA, "sweep-front launch did not form the requested clusters (results invalid)");
   if (e) return fail(ctx, LSW_ERR_CUDA, "a sweep-front kernel gave up on a bounded wait (results invalid)");
   return LSW_OK;
@@ -322,10 +332,6 @@ namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;   // 8 MiB
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
-
-// device address of g_noalloc_scratch per device, looked up once per device
-std::mutex g_noalloc_mu;
-void* g_noalloc_addr[256] = {};
 
 // writes the descriptors of `nrhs` full-cell right-hand sides of one cell:
 // items of at most rmax slots, each with its share of the forward storage
@@ -388,8 +394,35 @@ lsw_status lsw_ctx_create(lsw_ctx** out, int device) {
   if (const char* ev = std::getenv("LSW_KRYLOV_BATCH")) c->krylov_batch = std::max(0, std::atoi(ev));
   // LSW_FACTOR_LOOKAHEAD=0 factors each panel after the whole previous update
   if (const char* ev = std::getenv("LSW_FACTOR_LOOKAHEAD")) c->factor_lookahead = std::atoi(ev) != 0;
+  // the host-side name of the allocation-free solve's scratch array is not a
+  // device address: look the address up on this device (current since the
+  // cudaSetDevice above) and keep it with the context
+  e = cudaGetSymbolAddress(&c->noalloc_base, g_noalloc_scratch);
+  if (e != cudaSuccess || !c->noalloc_base) {
+    delete c;
+    return LSW_ERR_CUDA;
+  }
   *out = c;
   return LSW_OK;
+}
+
+lsw_status lsw_ctx_set_wait_limit(lsw_ctx* ctx, double seconds) {
+  if (!ctx) return LSW_ERR_INVALID_ARGUMENT;
+  if (!(seconds > 0.0) || !(seconds <= 60.0))
+    return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "wait limit must be in (0, 60] seconds");
+  int khz = 0;
+  if (cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, ctx->device) != cudaSuccess || khz <= 0) khz = 2070000;
+  ctx->wait_cycles = std::max(1000LL, (long long)(seconds * 1e3 * (double)khz));
+  return LSW_OK;
+}
+
+lsw_status lsw_selftest_bounded_wait(lsw_ctx* ctx, void* stream) {
+  if (!ctx) return LSW_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  if (!ctx->d_status.p) CK(ctx->d_status.ensure(16), "cudaMalloc(status)");
+  cudaStream_t st = S(stream);
+  KL(1, launch_wait_probe(ctx->d_status.as<int>() + 1, ctx->wait_cycles, st), "wait probe");
+  return check_kernel_err(ctx, st);
 }
 
 lsw_status lsw_ctx_destroy(lsw_ctx* ctx) {
@@ -505,11 +538,12 @@ lsw_status lsw_factorize(lsw_ctx* ctx, void* stream) {
                       ? launch_factorize<float>(ctx->d_cells.as<DevCell>(), ctx->ncell, ctx->d_prof.as<double2>(),
                                                 ctx->d_m.as<double>(), ctx->n_dof, w2, ctx->d_fac.p, ctx->d_work.p,
                                                 ctx->max_ny, ctx->d_status.as<int>(), st, ctx->prec == LSW_PREC_SPLIT,
-                                                ctx->factor_lookahead)
+                                                ctx->factor_lookahead, ctx->wait_cycles)
                       : launch_factorize<double>(ctx->d_cells.as<DevCell>(), ctx->ncell, ctx->d_prof.as<double2>(),
                                                  ctx->d_m.as<double>(), ctx->n_dof, w2, ctx->d_fac.p, ctx->d_work.p,
                                                  ctx->max_ny, ctx->d_status.as<int>(), st, false,
-                                                 false);   // complex128: the update dominates, no overlap
+                                                 false,   // complex128: the update dominates, no overlap
+                                                 ctx->wait_cycles);
   CK(e, "factorize kernel");
   int status = 0;
   CK(cudaMemcpyAsync(&status, ctx->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H status");
@@ -672,6 +706,7 @@ lsw_status lsw_local_solve(lsw_ctx* ctx, int cell, const void* b, void* x, int n
   a.item_count = (int)items.size();
   a.max_slots = std::min(rmax, nrhs);
   a.err = ctx->d_status.as<int>() + 1;
+  a.wait_cycles = ctx->wait_cycles;
   a.split = ctx->prec == LSW_PREC_SPLIT ? 1 : 0;
   a.cluster = fitting_cluster(ctx, a.max_slots, front_cluster(a.item_count, ctx->nsm, ctx->max_cluster));
   cudaError_t e = dbl ? launch_front<double>(a, ctx->max_ny, ctx->max_nx, st) : launch_front<float>(a, ctx->max_ny, ctx->max_nx, st);
@@ -1110,19 +1145,9 @@ lsw_status lsw_local_solve_noalloc(lsw_ctx* ctx, int cell, const void* b, void* 
                     std::to_string(cell) + " need " + std::to_string(need) + " bytes of scratch, more than the " +
                     std::to_string(kNoAllocScratchBytes) + "-byte fixed buffer; use fewer right-hand sides per call");
   }
-  // once per device, with that device current: the device address of the array
-  void* base = nullptr;
-  {
-    std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (ctx->device < 0 || ctx->device >= 256) return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "device index out of range");
-    if (!g_noalloc_addr[ctx->device]) {
-      void* p = nullptr;
-      CK(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(no-allocation scratch)");
-      g_noalloc_addr[ctx->device] = p;
-    }
-    base = g_noalloc_addr[ctx->device];
-  }
-  unsigned char* bp = static_cast<unsigned char*>(base);
+  // the array's device address on this context's device (lsw_ctx_create)
+  unsigned char* bp = static_cast<unsigned char*>(ctx->noalloc_base);
+  if (!bp) return fail(ctx, LSW_ERR_CUDA, "no-allocation scratch address unknown");
   DevItem* d_items = reinterpret_cast<DevItem*>(bp);
   DevSlot* d_slots = reinterpret_cast<DevSlot*>(bp + (size_t)n_items * sizeof(DevItem));
   void* d_scr = bp + desc_bytes;
@@ -1147,6 +1172,7 @@ lsw_status lsw_local_solve_noalloc(lsw_ctx* ctx, int cell, const void* b, void* 
   a.item_count = n_items;
   a.max_slots = std::min(rmax, nrhs);
   a.err = ctx->d_status.as<int>() + 1;
+  a.wait_cycles = ctx->wait_cycles;
   a.split = ctx->prec == LSW_PREC_SPLIT ? 1 : 0;
   a.cluster = fitting_cluster(ctx, a.max_slots, front_cluster(a.item_count, ctx->nsm, ctx->max_cluster));
   cudaError_t e = dbl ? launch_front<double>(a, ctx->max_ny, ctx->max_nx, st) : launch_front<float>(a, ctx->max_ny, ctx->max_nx, st);

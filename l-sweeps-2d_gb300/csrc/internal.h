@@ -164,6 +164,7 @@ struct FrontArgs {
   int chunk;              // factor columns per streamed chunk (set by the launcher)
   int ksw;                // consumer column slices (set by the launcher)
   int split;              // factors hold bf16 hi/lo terms; the matvec runs on mma.sync
+  long long wait_cycles;  // bounded-wait limit in clock cycles
 };
 // CTAs per half of an item (the item's cluster holds two halves) for a
 // front of `items` cell solves on `nsm` SMs, with at most `max_cta` CTAs per item
@@ -187,7 +188,10 @@ int front_fit_mask(bool dbl, bool split, int max_ny, int max_nx, int slots);
 template <typename T> cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* prof,
                                                    const double* mgrid, int n_dof, double omega2,
                                                    void* fac, void* prev, int max_ny, int* status,
-                                                   cudaStream_t st, bool split = false, bool lookahead = true);
+                                                   cudaStream_t st, bool split, bool lookahead,
+                                                   long long wait_cycles);
+// one bounded wait on a barrier that nothing completes (bit 1 of *err when it runs out)
+cudaError_t launch_wait_probe(int* err, long long limit_cycles, cudaStream_t st);
 size_t factor_smem_bytes(int ny, bool dbl);
 
 cudaError_t launch_apply_A(const double2* x, double2* y, int nrhs, int n_dof, const double2* gprof,

@@ -54,7 +54,6 @@ constexpr int kFT = 512;              // threads per CTA
 constexpr int kTX = 16, kTY = 32;     // update tile grid (columns x rows)
 constexpr int kRI = 6;                // rows per thread in the update: ny <= 192
 constexpr int kMaxN = kRI * kTY;
-constexpr long long kWaitCycles = 4000000000LL;   // ~2 s at 2 GHz
 constexpr unsigned kSuspendNs = 1000000;
 
 template <typename T> struct FacCfg;
@@ -208,7 +207,7 @@ __global__ void __launch_bounds__(kFT, 1)
 k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
             const double* __restrict__ mgrid, int n_dof, double omega2, cx_t<T>* __restrict__ fac,
             cx_t<T>* __restrict__ prev, long long prev_stride, int split, int middle, int lookahead, int G,
-            int nmax, int ldw, int* status) {
+            int nmax, int ldw, int* status, long long wait_cycles) {
   using C = cx_t<T>;
   constexpr int CJ = FacCfg<T>::CJ;
   constexpr int kB = FacCfg<T>::B;
@@ -233,6 +232,7 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 8);
   unsigned* wkey = reinterpret_cast<unsigned*>(smem + 16);    // [2][8] per-warp pivot keys by step parity
+  uint64_t* exitbar = reinterpret_cast<uint64_t*>(smem + 128); // every CTA of the cluster is done
   int* used = reinterpret_cast<int*>(smem + 256);             // [nmax]
   int* piv = used + kMaxN;                                     // [nmax]
   int* pslot = piv + kMaxN;                                    // [nmax] block pivot slot of a row, -1 if none
@@ -256,6 +256,7 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
   if (tid == 0) {
     *abort_flag = 0;
     mbar_init(bar, (unsigned)G);
+    mbar_init(exitbar, (unsigned)G);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   for (int i = tid; i < kMaxN; i += kFT) pslot[i] = -1;
@@ -275,7 +276,7 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
       const long long t0 = clock64();
       while (!(ok = mbar_try_wait_cluster(bar, phase & 1u))) {
         if (*abort_flag) break;
-        if (clock64() - t0 > kWaitCycles) {
+        if (clock64() - t0 > wait_cycles) {
           *abort_flag = 1;
           atomicOr(status, 2);
           break;
@@ -285,6 +286,23 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
     ++phase;
     __syncthreads();
     return *abort_flag == 0;
+  };
+  // Before leaving, normally or after a wait gave up: every CTA arrives on
+  // every CTA's exit barrier and waits for its own, bounded by the limit
+  // alone, so that no CTA leaves while a peer may still read its shared
+  // memory (the panel columns, pivots and reciprocals).
+  auto leave = [&]() {
+    __syncthreads();
+    if (G == 1) return;
+    if (tid < G) mbar_arrive_remote(exitbar, (unsigned)tid);
+    if (mbar_try_wait_cluster(exitbar, 0u)) return;
+    const long long t0 = clock64();
+    while (!mbar_try_wait_cluster(exitbar, 0u)) {
+      if (clock64() - t0 > wait_cycles) {
+        atomicOr(status, 2);
+        break;
+      }
+    }
   };
 
   for (int step = 0; step < nsteps; ++step) {
@@ -464,7 +482,7 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
       const int k2 = more ? min(k1 + kB, (o2 + 1) * n / G) : k1;
 
       if (cur) {
-        if (!csync()) return;
+        if (!csync()) { leave(); return; }
         if ((int)g != o) {
           // the panel owner's columns f_t, pivots and reciprocals
           for (int e = tid; e < bt * n; e += kFT) {
@@ -542,8 +560,9 @@ k_factorize(const DevCell* __restrict__ cells, const double2* __restrict__ prof,
       Fk[(size_t)j * ldn + i] = v;
     }
     // the next line's Schur complement reads every CTA's columns of Sinv_k
-    if (!csync()) return;
+    if (!csync()) { leave(); return; }
   }
+  leave();
 }
 
 template <typename T>
@@ -583,7 +602,7 @@ size_t factor_smem_bytes(int ny, bool dbl) {
 template <typename T>
 cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* prof, const double* mgrid,
                              int n_dof, double omega2, void* fac, void* prev, int max_ny, int* status,
-                             cudaStream_t st, bool split, bool lookahead) {
+                             cudaStream_t st, bool split, bool lookahead, long long wait_cycles) {
   if (ncell <= 0) return cudaSuccess;
   if (max_ny > kMaxN) return cudaErrorInvalidValue;
   int dev = 0, maxopt = 0, ldw = 0;
@@ -617,7 +636,7 @@ cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* pro
     cfg.gridDim = dim3((unsigned)(ncell * G * (middle ? 1 : 2)));
     e = cudaLaunchKernelEx(&cfg, kern, cells, prof, mgrid, n_dof, omega2, reinterpret_cast<cx_t<T>*>(fac),
                            reinterpret_cast<cx_t<T>*>(split ? prev : nullptr), prev_stride, split ? 1 : 0, middle,
-                           lookahead ? 1 : 0, G, max_ny, ldw, status);
+                           lookahead ? 1 : 0, G, max_ny, ldw, status, wait_cycles);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -625,8 +644,8 @@ cudaError_t launch_factorize(const DevCell* cells, int ncell, const double2* pro
 
 
 template cudaError_t launch_factorize<float>(const DevCell*, int, const double2*, const double*, int, double,
-                                             void*, void*, int, int*, cudaStream_t, bool, bool);
+                                             void*, void*, int, int*, cudaStream_t, bool, bool, long long);
 template cudaError_t launch_factorize<double>(const DevCell*, int, const double2*, const double*, int, double,
-                                              void*, void*, int, int*, cudaStream_t, bool, bool);
+                                              void*, void*, int, int*, cudaStream_t, bool, bool, long long);
 
 }  // namespace lsw

@@ -78,7 +78,6 @@ constexpr int kAux = 4;               // producer, two helper warps, writer warp
 constexpr int kNSMax = 8;             // ring stages
 constexpr int kHdr = 256;             // barrier header bytes
 constexpr int SK_NONE = 99;           // padding slot
-constexpr long long kWaitCycles = 4000000000LL;   // ~2 s at 2 GHz
 constexpr unsigned kSuspendNs = 1000000;          // try_wait sleeps up to 1 ms (woken by the phase)
 
 
@@ -136,17 +135,20 @@ __device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t* b, unsigned pari
       : "memory");
   return ok != 0;
 }
-// Bounded wait (see the file comment).
+// Bounded wait (see the file comment): gives up after `limit` clock cycles,
+// or at once when the CTA's abort flag is up (abort_flag == nullptr: a wait
+// that only the limit ends, for the drain before leaving).
 template <bool CLUSTER>
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity, int* err, volatile int* abort_flag) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity, int* err, volatile int* abort_flag,
+                                          long long limit) {
   auto tw = [&]() { return CLUSTER ? mbar_try_wait_cluster(b, parity) : mbar_try_wait(b, parity); };
   if (tw()) return true;
   const long long t0 = clock64();
   while (true) {
-    if (*abort_flag) return false;
+    if (abort_flag && *abort_flag) return false;
     if (tw()) return true;
-    if (clock64() - t0 > kWaitCycles) {
-      *abort_flag = 1;
+    if (clock64() - t0 > limit) {
+      if (abort_flag) *abort_flag = 1;
       atomicOr(err, 2);
       return false;
     }
@@ -550,13 +552,17 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   if (warp == 0) {
     if (lane < 2) {
       long long idx = 0;
-      for (int li = 0; li < nline; ++li) {
+      bool stopped = false;
+      for (int li = 0; li < nline && !stopped; ++li) {
         const C* blk = fac + (size_t)line_k(li) * ny * ldn;
         for (int c = 0; c < nch; ++c, ++idx) {
           if ((idx & 1) != lane) continue;   // lanes 0 and 1 issue alternate chunks
           const int slot = (int)(idx % NS);
           if (idx >= NS) {
-            if (!mbar_wait<false>(&empty[slot], (unsigned)(((idx / NS) - 1) & 1), a.err, abort_flag)) return;
+            if (!mbar_wait<false>(&empty[slot], (unsigned)(((idx / NS) - 1) & 1), a.err, abort_flag, a.wait_cycles)) {
+              stopped = true;
+              break;
+            }
           }
           const int c0 = jb + c * CW;
           const int ncol = min(CW, je - c0);
@@ -565,6 +571,12 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
           bulk_g2s(ring + (size_t)slot * slot_elems, blk + (size_t)c0 * ldn, bytes, &full[slot]);
         }
       }
+      // Wait (bounded by the limit alone) until the last copies this lane
+      // issued have landed: after an abort the consumers stop waiting for
+      // them, and no copy may write into shared memory after the CTA has left.
+      // Without an abort they landed long ago and each wait returns at once.
+      for (long long q = max(0LL, idx - NS); q < idx; ++q)
+        if ((q & 1) == lane) mbar_wait<false>(&full[(int)(q % NS)], (unsigned)((q / NS) & 1), a.err, nullptr, a.wait_cycles);
     }
     return;
   }
@@ -680,7 +692,7 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
       const int g = lane >> 2, t = lane & 3, mb = cw * 16;
       for (int c = 0; c < nch; ++c, ++idx) {
         const int slot = (int)(idx % NS);
-        const bool ok = mbar_wait<false>(&full[slot], (unsigned)((idx / NS) & 1), a.err, abort_flag);
+        const bool ok = mbar_wait<false>(&full[slot], (unsigned)((idx / NS) & 1), a.err, abort_flag, a.wait_cycles);
         const uint2* S2 = reinterpret_cast<const uint2*>(ring + (size_t)slot * slot_elems) + mb + g;
         const int c0 = c * CW;
         const int nks = (min(CW, nJ - c0) + 7) >> 3;
@@ -730,7 +742,7 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
       for (int r = 0; r < R; ++r) { acc0[r] = czero<C>(); acc1[r] = czero<C>(); }
       for (int c = 0; c < nch; ++c, ++idx) {
         const int slot = (int)(idx % NS);
-        const bool ok = mbar_wait<false>(&full[slot], (unsigned)((idx / NS) & 1), a.err, abort_flag);
+        const bool ok = mbar_wait<false>(&full[slot], (unsigned)((idx / NS) & 1), a.err, abort_flag, a.wait_cycles);
         const C* S = ring + (size_t)slot * slot_elems + r0;
         const int c0 = c * CW;
         const int ncol = min(CW, nJ - c0);
@@ -791,7 +803,7 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
         }
       }
     }
-    if (CL > 1) mbar_wait<true>(&pready[buf], (unsigned)((li >> 1) & 1), a.err, abort_flag);
+    if (CL > 1) mbar_wait<true>(&pready[buf], (unsigned)((li >> 1) & 1), a.err, abort_flag, a.wait_cycles);
     named_sync(1, NSYNC);     // sync1: partials (cluster-wide) and H complete
 
     // ---- finish the line for my rows, element-wise ----
@@ -820,7 +832,7 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
       if (last) {
         // middle input b_m - w_m y_{m-1} - e_m z_{m+1}, formed in the same
         // order in both halves so that both compute the same x_m
-        mbar_wait<true>(xch, 0u, a.err, abort_flag);
+        mbar_wait<true>(xch, 0u, a.err, abort_flag, a.wait_cycles);
         const C wm = wsh[mid], em = esh[mid];
         for (int e = ct; e < R * nJ; e += NCT) {
           const C own = Y[e], oth = P[e];
@@ -863,7 +875,9 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
     // nobody leaves while a peer may still write into its shared memory
     __syncwarp();
     if (lane < CLT) mbar_arrive_remote(&exitb[0], (unsigned)lane);
-    mbar_wait<true>(&exitb[0], 0u, a.err, abort_flag);
+    // waited on even after an abort (bounded by the limit alone): a peer
+    // still pushing partial sums into this CTA's shared memory keeps it alive
+    mbar_wait<true>(&exitb[0], 0u, a.err, nullptr, a.wait_cycles);
   }
 }
 
@@ -1028,6 +1042,28 @@ int front_max_clusters(bool dbl, int cluster) {
     return 0;
   }
   return n;
+}
+
+namespace {
+// One CTA waits on an mbarrier that nothing completes, with the bounded wait
+// of the sweep kernels: the wait runs out after `limit` cycles, raises the
+// error word and the kernel returns normally (no trap, nothing in flight).
+__global__ void k_wait_probe(int* err, long long limit) {
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int abort_flag;
+  if (threadIdx.x == 0) {
+    abort_flag = 0;
+    mbar_init(&bar, 1);   // expects one arrive that never comes
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) mbar_wait<false>(&bar, 0u, err, &abort_flag, limit);
+  __syncthreads();
+}
+}  // namespace
+
+cudaError_t launch_wait_probe(int* err, long long limit_cycles, cudaStream_t st) {
+  k_wait_probe<<<1, 32, 0, st>>>(err, limit_cycles);
+  return cudaGetLastError();
 }
 
 template cudaError_t launch_front<float>(const FrontArgs&, int, int, cudaStream_t);

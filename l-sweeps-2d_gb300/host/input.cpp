@@ -377,12 +377,17 @@ void Input::readProblemSolver(GlobalIterativeSolver*& solver, UInt probID) const
   if (!sol.lookupValue("Type", type)) need("Type in GlobalSolver " + name);
   if (type != "GMRES") throw lsw_host_error("ERROR: unknown global solver " + type);
   auto* g = new GlobalIterativeSolverGMRES();
-  double tol;
-  UInt maxIter, restart;
-  bool verbose;
-  if (sol.lookupValue("Tol", tol)) g->setTol(tol);
-  if (sol.lookupValue("MaxIter", maxIter)) g->setMaxIter(maxIter);
-  if (sol.lookupValue("Verbose", verbose)) g->setVerbose(verbose);
+  // as Input::readProblemSolver reads them (Input.cpp:367-387): Tol = 0 and
+  // MaxIter = 0 keep the solver's defaults (1e-6, 40), Verbose defaults to true
+  double tol = 1.0e-6;
+  UInt maxIter = 0, restart;
+  bool verbose = true;
+  sol.lookupValue("Tol", tol);
+  sol.lookupValue("MaxIter", maxIter);
+  sol.lookupValue("Verbose", verbose);
+  if (tol != 0.0) g->setTol(tol);
+  if (maxIter != 0) g->setMaxIter(maxIter);
+  if (!verbose) g->setVerbose(false);
   // extensions: Mode = "reference" (default) | "flexible", Restart
   std::string mode;
   if (sol.lookupValue("Mode", mode)) {

@@ -22,6 +22,7 @@ EXPORTS = [
     "lsw_problem_setup", "lsw_problem_info_get", "lsw_cell_info_get", "lsw_factorize", "lsw_apply_precond",
     "lsw_apply_A", "lsw_assemble_rhs", "lsw_gmres", "lsw_solve_host", "lsw_local_solve",
     "lsw_apply_precond_profiled", "lsw_local_solve_noalloc", "lsw_release_workspace",
+    "lsw_ctx_set_wait_limit", "lsw_selftest_bounded_wait",
 ]
 
 
@@ -103,6 +104,8 @@ def lib() -> C.CDLL:
         "lsw_apply_precond_profiled": (i, [vp, vp, vp, i, vp, C.POINTER(ApplyProfile)]),
         "lsw_local_solve_noalloc": (i, [vp, i, vp, vp, i, vp]),
         "lsw_release_workspace": (i, [vp]),
+        "lsw_ctx_set_wait_limit": (i, [vp, d]),
+        "lsw_selftest_bounded_wait": (i, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -147,7 +147,13 @@ class GpuOperator:
     def __init__(self, spec: ProblemSpec, m_grid: np.ndarray, precision: str, device: int, stream):
         from .solver import Solver
         self.solver = Solver(spec, m_grid, precision=precision, device=device)
-        self.solver.factorize(stream=stream)
+        try:
+            self.solver.factorize(stream=stream)
+        except BaseException:
+            # a failed factorisation (e.g. out of device memory) returns its
+            # context and buffers now, not when the exception is collected
+            self.solver.close()
+            raise
         self.bytes = int(self.solver.info()["device_bytes"])
 
     def solve(self, reqs: list, stream, restart: int = 30, max_iter: int = 400) -> None:
@@ -192,6 +198,12 @@ class GpuBackend:
 
     def create(self, req: Request, stream):
         return GpuOperator(req.spec, req.medium.build(req.spec), req.precision, self.device, stream)
+
+    def trim(self) -> None:
+        """Return torch's cached, unused device blocks to the driver (before an
+        out-of-memory retry)."""
+        import torch
+        torch.cuda.empty_cache()
 
 
 # ---------------------------------------------------------------------------
@@ -355,21 +367,29 @@ class ServeEngine:
     def _oom_retry(self, e, fn):
         """Run fn; if the device ran out of memory (the footprint estimate was
         low), evict every idle operator but e and run it once more."""
+        oom = False
         try:
             return fn()
         except Exception as ex:
             if "OUT_OF_MEMORY" not in str(ex) and "out of memory" not in str(ex).lower():
                 raise
-            with self._cv:
-                victims = [x for x in self.cache.entries.values() if not x.busy and x is not e]
-                for v in victims:
-                    del self.cache.entries[v.key]
-                    self.cache.evictions += 1
-                self._oom_retries += 1
+            oom = True
+        # retried outside the handler: the failed call's frames (and the device
+        # buffers they hold) are released with the exception before the retry
+        assert oom
+        with self._cv:
+            victims = [x for x in self.cache.entries.values() if not x.busy and x is not e]
             for v in victims:
-                if v.op is not None:
-                    v.op.close()
-            return fn()
+                del self.cache.entries[v.key]
+                self.cache.evictions += 1
+            self._oom_retries += 1
+        for v in victims:
+            if v.op is not None:
+                v.op.close()
+        trim = getattr(self.backend, "trim", None)
+        if trim is not None:
+            trim()
+        return fn()
 
     def _worker(self, slot: int):
         stream = self.backend.new_stream()

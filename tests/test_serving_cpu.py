@@ -218,3 +218,66 @@ def test_percentiles_and_stream_generator():
     assert len(set(keys)) < len(keys)          # some media repeat
     assert all(1 <= len(r.sources) <= 16 for r in s)
     assert {r.spec.N for r in s} <= {2, 4}
+
+
+class PartialCreateBackend(FakeBackend):
+    """create() allocates (a handle that must be closed) and then runs out of
+    memory once, as a factorisation would; the retry succeeds."""
+
+    def __init__(self):
+        super().__init__()
+        self.failed = False
+        self.trims = 0
+
+    def create(self, req, stream):
+        if req.rid == 1 and not self.failed:
+            self.failed = True
+            self.log.append(("alloc-partial", req.key()))
+            try:
+                raise RuntimeError("LSW_ERR_OUT_OF_MEMORY: cudaMalloc(factors): out of memory")
+            except RuntimeError:
+                self.log.append(("close-partial", req.key()))
+                raise
+        return FakeOp(req, self.log, self.factor_s)
+
+    def trim(self):
+        self.trims += 1
+        self.log.append(("trim",))
+
+
+def test_out_of_memory_on_create_closes_partial_operator_before_retry():
+    be = PartialCreateBackend()
+    eng = ServeEngine(be, slots=1, max_batch=4, budget=10 * one_op_bytes())
+    seq = [_req(0, 0, 0.00), _req(1, 1, 0.05)]
+    st = eng.run(seq, realtime=True)
+    assert st.n == 2 and st.failures == 0 and st.oom_retries == 1
+    kinds = [e[0] for e in be.log]
+    # the partial operator is closed, the cache trimmed, and only then created again
+    i_close = kinds.index("close-partial")
+    i_trim = kinds.index("trim")
+    i_create = max(i for i, e in enumerate(be.log) if e[0] == "create" and e[1] == seq[1].key())
+    assert i_close < i_trim < i_create
+    assert seq[1].x is not None
+
+
+def test_gpu_operator_closes_its_solver_when_factorisation_fails(monkeypatch):
+    """GpuOperator returns its context when factorize raises (no GPU: the
+    Solver is replaced by a recording fake)."""
+    import lsweeps.solver as solver_mod
+    from lsweeps.serving import GpuOperator
+    events = []
+
+    class FakeSolver:
+        def __init__(self, *a, **k):
+            events.append("init")
+
+        def factorize(self, stream=None):
+            raise RuntimeError("LSW_ERR_OUT_OF_MEMORY: cudaMalloc(factors): out of memory")
+
+        def close(self):
+            events.append("close")
+
+    monkeypatch.setattr(solver_mod, "Solver", FakeSolver)
+    with pytest.raises(RuntimeError):
+        GpuOperator(_spec(), np.ones((1, 1)), "c64", 0, None)
+    assert events == ["init", "close"]

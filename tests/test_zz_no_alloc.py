@@ -1,5 +1,7 @@
 """The allocation-free cell solve (lsw_local_solve_noalloc) gives the same
-result as lsw_local_solve, through the C ABI, on two calls in a row.
+result as lsw_local_solve, through the C ABI, on two calls in a row: bit for
+bit (the same kernel and launch shape; only where the scratch lives differs),
+and within the precision's tolerance of the oracle's SuperLU cell solve.
 
 It serves callers that cannot call cudaMalloc (a fixed device-memory budget
 owned by their own pool, or loops that cannot afford an allocation's device
@@ -26,9 +28,11 @@ def _rel(a, b):
 @pytest.mark.parametrize("prec,tol", [("c128", 1e-10), ("c64", 2e-4), ("bf16x2", 2e-4)])
 def test_noalloc_local_solve_matches_local_solve(prec, tol):
     from lsweeps.solver import Solver, _stream_ptr
+    from oracle.lsweeps_oracle import OracleProblem
     spec, med = small(N=3, m=12, p=5, medium="layered", seed=2)
     S = Solver(spec, med, precision=prec)
     S.factorize()
+    P = OracleProblem(spec.N, spec.m, spec.p, spec.h, spec.omega, med)
     L = capi.lib()
     rng = np.random.default_rng(21)
     for call, (cell, nrhs) in enumerate(((4, 3), (0, 5))):   # two calls in a row
@@ -44,7 +48,14 @@ def test_noalloc_local_solve_matches_local_solve(prec, tol):
         torch.cuda.synchronize()
         got = x.cpu().numpy()
         assert np.isfinite(got).all()
-        assert _rel(got, ref) <= tol, f"call {call}"
+        # the same kernel and launch shape as lsw_local_solve: identical bits
+        assert np.array_equal(got, ref), f"call {call}: {_rel(got, ref):.3e}"
+        # and the oracle's SuperLU solve of the same cell
+        oc = P.dd.cells[cell]
+        oc.factorize()
+        assert oc.size == n
+        want = np.concatenate([oc.solve(b[r * n:(r + 1) * n]) for r in range(nrhs)])
+        assert _rel(got, want) <= tol, f"call {call} vs SuperLU"
 
 
 def test_noalloc_rejects_oversized_request():
