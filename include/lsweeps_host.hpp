@@ -2,7 +2,7 @@
  * liblsweeps_gb300.so (lsweeps.h).
  *
  * The classes keep the names, virtuals and call pattern of the reference
- * (L-Sweeps-2D, include/*.h) so that its driver code (main.cpp,
+ * (L-Sweeps-2D, the headers under include/) so that its driver code (main.cpp,
  * src/Problem.cpp) compiles against them: a DDCheckerboard is set up from an
  * AssemblerHelmholtz2DFD (omega, PMLCubic2D, squared slowness Function), a
  * LocalLinearSolver prototype (LocalLinearSolverCUDA beside the reference's
