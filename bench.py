@@ -46,6 +46,12 @@ WORKLOAD = WORKLOADS["C4"]
 # factor and sweep arithmetic per workload: complex FP32 where the workload names it, the
 # BF16-split tensor-core products (hi + lo bf16 terms, FP32 accumulation) for the 4096^2 case
 PRECISION = {"C1": "c64", "C2": "c64", "C3": "c64", "C4": "bf16x2"}
+DATA = {"C1": "synthetic (constant medium)", "C2": "synthetic (seeded Gaussian-lens medium)",
+        "C3": "synthetic (seeded layered medium)", "C4": "synthetic (seeded piecewise-smooth random medium)"}
+# how L2 is kept out of the timing: every workload streams more factor bytes per apply than L2 holds
+L2_NOTE = {n: f"inputs larger than L2 (129 MB): {gb} of cell factors streamed per preconditioner apply"
+           for n, gb in (("C1", "0.1 GB"), ("C2", "2.3 GB (c64)"), ("C3", "10.7 GB (c64)"),
+                         ("C4", "43.9 GB (bf16x2)"))}
 DTYPE = {"c64": "c64 factors/applies + f64 Krylov",
          "bf16x2": "bf16-split factor products (hi+lo, fp32 accumulate) + f64 Krylov",
          "c128": "c128 factors/applies + f64 Krylov"}
@@ -135,136 +141,118 @@ def max_over_ranks(x: float, dist=None, device="cpu") -> float:
     return float(t.item())
 
 
-def _interior_cell(spec, med):
-    """One interior C2-shaped cell (column/row 1: interior domain [a - 2h, b + 4h],
-    (m + 6 + 2p - 1)^2 DOFs), assembled by the oracle."""
-    from oracle.lsweeps_oracle import AssemblerHelmholtz2DFD, SubdomainStructured, grid_medium
-    h, m = spec.h, spec.m
-    a = (m + 1) * h
-    dom = ((a - 2 * h, a + m * h + 4 * h), (a - 2 * h, a + m * h + 4 * h))
-    asm = AssemblerHelmholtz2DFD(spec.omega, spec.p * h, grid_medium(med, h, spec.p))
-    asm.set_domain(dom)
-    asm.set_n((m + 6, m + 6))
-    cell = SubdomainStructured(asm, 1, 1)
-    cell.A = asm.assemble_system_matrix()
-    cell.size = cell.A.shape[0]
-    return cell
+def reference_iterations(name: str) -> dict:
+    """The reference GMRES's iteration count on a workload (committed fixture,
+    tests/golden/make_reference_iterations.py)."""
+    f = ROOT / "tests" / "golden" / "reference_gmres_iterations.json"
+    return json.loads(f.read_text())[name]
 
 
-def _cell_solve_worker(spec, med, budget_s: float, barrier, results) -> None:
-    """A worker process of the all-core sample: factorise the cell, wait for
-    every worker, then solve for `budget_s`; reports the solves done."""
+def reference_sample(spec, name: str, med, parts: int, warmup_parts: int = 0, procs: int | None = None,
+                     log=None) -> dict:
+    """Time the oracle's restatement of the reference on the host cores: the
+    DDCheckerboard apply (DDCheckerboard::applyPrecond, DDCheckerboard.cpp:
+    687-739) with its cell solves spread over worker processes that own rows
+    of cells round-robin (the reference's MPI layout,
+    DDCheckerboard.cpp:126-177; SuperLU, one thread each), front by front as
+    the reference's pipelined sweeps run them.  `parts` timed shifted parts
+    (one of the four shifted decompositions each, in turn) give the apply time;
+    the DD matvec, the Arnoldi dot and axpy on the global vectors are timed
+    once.  A reference solve of k iterations (GlobalIterativeSolverGMRES.cpp:
+    65-203) costs k + 2 applies (75, 82, 255), k + 1 matvecs and
+    sum_{j<k} (j + 1) dot + axpy pairs."""
     import numpy as np
-    cell = _interior_cell(spec, med)
-    cell.factorize()
-    rng = np.random.default_rng(os.getpid())
-    b = rng.standard_normal(cell.size) + 1j * rng.standard_normal(cell.size)
-    barrier.wait()
-    t_end = time.perf_counter() + budget_s
-    k = 0
-    while time.perf_counter() < t_end:
-        cell.solve(b)
-        k += 1
-    results.put(k)
-
-
-def cpu_sample(spec, med, iterations: int, budget_s: float = 25.0, procs: int | None = None) -> dict:
-    """Time the oracle's cell solves (SuperLU) on a sample of the C2 cells and
-    extrapolate to one preconditioner apply (the apply is a sum of cell solves:
-    N^2 + 4N(N-1) + 4(N-1)^2 per shifted decomposition, x4) and to one solve of
-    `iterations` FGMRES iterations (iterations + 1 applies).  With procs > 1,
-    `procs` spawned processes (one thread each) solve concurrently for the
-    budget and their aggregate rate gives the per-solve time: the solves of a
-    sweep front are independent (C2: >= 64 per front step), as the
-    reference's ranks run them."""
-    import numpy as np
-    procs = procs if procs is not None else (os.cpu_count() or 1)
+    from oracle.parallel import ParallelOracle
+    procs = procs or os.cpu_count() or 1
+    k = reference_iterations(name)["iterations"]
     t0 = time.perf_counter()
-    cell = _interior_cell(spec, med)
-    setup_s = time.perf_counter() - t0
-    t1 = time.perf_counter()
-    cell.factorize()
-    fact_s = time.perf_counter() - t1
-    rng = np.random.default_rng(0)
-    n = cell.size
-    ts, k = [], 0
-    t2 = time.perf_counter()
-    single_s = min(3.0, budget_s / 3) if procs > 1 else budget_s
-    while time.perf_counter() - t2 < single_s and k < 400:
-        b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    with ParallelOracle(spec.N, spec.m, spec.p, spec.h, spec.omega, med, procs=procs) as Q:
+        setup_s = time.perf_counter() - t0
+        procs = Q.procs   # at most one worker per row of cells, as the reference's ranks
+        rng = np.random.default_rng(0)
+        n2 = Q.n_dof ** 2
+        xc = Q.cells_of(rng.standard_normal(n2) + 1j * rng.standard_normal(n2))
+        per_q = {0: [], 1: [], 2: [], 3: []}
+        steps = []
+        for i in range(warmup_parts + parts):
+            q = i % 4
+            t = time.perf_counter()
+            res = Q.dd.apply_precond_part(xc, q)
+            dt = time.perf_counter() - t
+            if i >= warmup_parts:
+                per_q[q].append(dt)
+                steps.append(dt)
+            if log:
+                log(f"part {q}: {dt:.2f} s")
+        for q in range(4):   # parts never timed: their warm-up times
+            if not per_q[q]:
+                t = time.perf_counter()
+                Q.dd.apply_precond_part(xc, q)
+                per_q[q].append(time.perf_counter() - t)
         t = time.perf_counter()
-        cell.solve(b)
-        ts.append(time.perf_counter() - t)
-        k += 1
-    t_solve = statistics.median(ts)
-    N = spec.N
-    n_solves = 4 * (N * N + 4 * N * (N - 1) + 4 * (N - 1) ** 2)
-    par = ""
-    cores = 1
-    t_cell = t_solve
-    if procs > 1:
-        import multiprocessing as mp
-        # spawned workers (never forked after a GPU call), one BLAS thread each
-        par_s = budget_s / 2
-        ctx = mp.get_context("spawn")
-        saved = {v: os.environ.get(v) for v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")}
-        for v in saved:
-            os.environ[v] = "1"
-        try:
-            barrier, results = ctx.Barrier(procs), ctx.Queue()
-            ws = [ctx.Process(target=_cell_solve_worker, args=(spec, med, par_s, barrier, results))
-                  for _ in range(procs)]
-            for w in ws:
-                w.start()
-            counts = [results.get(timeout=600) for _ in ws]
-            for w in ws:
-                w.join()
-        finally:
-            for v, old in saved.items():
-                if old is None:
-                    os.environ.pop(v, None)
-                else:
-                    os.environ[v] = old
-        total = sum(counts)
-        if total > 0:
-            t_cell = par_s / total               # amortised per-solve time with every worker busy
-            cores = procs
-            par = (f"; all-core rate: {procs} processes x {par_s:.1f} s, {total} solves "
-                   f"({t_cell * 1e3:.3f} ms per solve amortised, {t_solve / t_cell:.1f}x one process)")
-    t_apply = n_solves * t_cell
-    t_sol = (iterations + 1) * t_apply
+        ax = Q.dd.apply_system_matrix(xc)
+        t_mv = time.perf_counter() - t
+        del res, ax
+    a = np.concatenate(xc)
+    b = a[::-1].copy()
+    td, ta = [], []
+    for _ in range(3):
+        t = time.perf_counter()
+        np.vdot(a, b)
+        td.append(time.perf_counter() - t)
+        t = time.perf_counter()
+        b = b - 0.5 * a
+        ta.append(time.perf_counter() - t)
+    t_dot, t_axpy = statistics.median(td), statistics.median(ta)
+    t_apply = sum(statistics.median(per_q[q]) for q in range(4))
+    t_krylov = (k + 1) * t_mv + sum(j + 1 for j in range(k)) * (t_dot + t_axpy)
+    t_solve = (k + 2) * t_apply + t_krylov
     return {
-        "value": 1.0 / t_sol, "unit": UNIT, "cores": cores, "kind": "port",
-        "sample": (f"oracle (numpy/SciPy SuperLU, one thread per process): {k} single-process solves of one "
-                   f"interior C2-shaped cell ({n} DOFs, median {t_solve * 1e3:.2f} ms){par}; x {n_solves} cell "
-                   f"solves per apply x {iterations + 1} applies per solve; cell factorisation {fact_s:.2f} s "
-                   f"x {N * N} cells not included (factors resident on both sides)"),
-        "t_apply_s": t_apply, "t_solve_s": t_sol, "cell_factorize_s": fact_s, "setup_s": setup_s,
+        "value": 1.0 / t_solve, "unit": UNIT, "cores": procs, "kind": "port",
+        "sample": (f"timed apply: the oracle's restatement of DDCheckerboard::applyPrecond on {name} "
+                   f"({spec.N}x{spec.N} cells, {Q.n_dof}^2 DOFs) with its SuperLU cell solves on {procs} "
+                   f"worker processes owning rows of cells round-robin (the reference's MPI layout), front by "
+                   f"front; {len(steps)} timed shifted parts (one of the four shifted decompositions each): "
+                   f"apply {t_apply:.2f} s; DD matvec {t_mv:.2f} s, dot {t_dot * 1e3:.1f} ms, axpy "
+                   f"{t_axpy * 1e3:.1f} ms on the global vectors; a reference GMRES solve of {k} iterations "
+                   f"(committed count) = {k + 2} applies + {k + 1} matvecs + {k * (k + 1) // 2} MGS dot/axpy "
+                   f"pairs = {t_solve:.1f} s; cell factorisation ({Q.factorize_s:.1f} s per worker) not "
+                   f"included (factors resident on both sides)"),
+        "t_apply_s": t_apply, "t_solve_s": t_solve, "iterations": k, "setup_s": setup_s,
+        "step_s": steps, "t_matvec_s": t_mv,
     }
+
+
+def bench_config(name: str, nrhs: int, world: int) -> dict:
+    """The workload description shared by both arms."""
+    from lsweeps.problems import config as _cfg
+    return {"workload": WORKLOADS[name], "restart": 30, "tol": 1e-6, "parallelism": f"replicas x{world}",
+            "nrhs": nrhs, "l2": L2_NOTE[name]}
 
 
 def run_reference(args):
     """--impl reference: the CPU restatement of the reference path, timed on
-    the host cores; rank 0 only."""
+    the host cores (every core, one worker process each); rank 0 only.  Each
+    step is one shifted part of a preconditioner apply of the workload (see
+    reference_sample)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     from lsweeps.problems import config
-    spec, med = config("C2")
-    its = args.ref_iterations
-    samples = []
-    for _ in range(max(1, args.warmup)):
-        cpu_sample(spec, med, its, budget_s=2.0, procs=1)
-    for _ in range(args.steps):
-        samples.append(cpu_sample(spec, med, its, budget_s=args.ref_budget))
-    vals = [s["value"] for s in samples]
-    v = statistics.median(vals)
+    name = args.config.upper()
+    spec, med = config(name)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    smp = reference_sample(spec, name, med, parts=args.steps, warmup_parts=args.warmup,
+                           log=lambda m: print(m, file=sys.stderr, flush=True))
+    v = smp["value"]
+    nrhs = len(spec.sources) if name == "C3" else 1
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "iterations_assumed": its},
-        "cpu_baseline": {k: samples[-1][k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(smp["step_s"]),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "data": DATA[name], "config": bench_config(name, nrhs, world),
+        "precision": "fp64 (reference arithmetic)", "iterations": smp["iterations"],
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": smp["cores"], "kind": "port", "sample": smp["sample"]},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -288,7 +276,6 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
 
     spec, med = config(args.config)
-    WORKLOAD = WORKLOADS[args.config.upper()]
     prec = args.precision or PRECISION[args.config.upper()]
     S = Solver(spec, med, precision=prec, device=local)
     st = torch.cuda.current_stream()
@@ -402,7 +389,10 @@ def run_gpu(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_sample(spec, med, reps[-1].iterations, budget_s=args.ref_budget)
+        # the Krylov bases and factors go first: the oracle's workers hold the
+        # cell factors in host memory, not on the GPU, but this keeps the
+        # process's footprint to the solver it timed
+        cpu = reference_sample(spec, args.config.upper(), med, parts=4)
         cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
 
     clocks = clk.summary()
@@ -412,15 +402,10 @@ def run_gpu(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_total * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[prec],
-            "data": {"C1": "synthetic (constant medium)", "C2": "synthetic (seeded Gaussian-lens medium)",
-                     "C3": "synthetic (seeded layered medium)",
-                     "C4": "synthetic (seeded piecewise-smooth random medium)"}[args.config.upper()],
-            "config": {"workload": WORKLOAD, "precision": "mixed" if prec != "c128" else "fp64",
-                       "factor_precision": prec, "restart": 30, "tol": args.tol,
-                       "parallelism": f"replicas x{world}",
-                       "nrhs": nrhs,
-                       "l2": f"inputs larger than L2: {S.info()['factor_bytes'] / 1e9:.1f} GB of {prec} factors "
-                             "streamed per apply (L2 129 MB)"},
+            "data": DATA[args.config.upper()],
+            "config": bench_config(args.config.upper(), nrhs, world),
+            "precision": "mixed" if prec != "c128" else "fp64", "factor_precision": prec,
+            "factor_bytes": S.info()["factor_bytes"],
             "p50_ms": p50, "p99_ms": pctl(step_ms, 0.99), "iterations": reps[-1].iterations,
             "true_rel_res": reps[-1].true_rel_res, "factorize_s": fact_s,
             "time_to_solution_s": fact_s + p50 / 1e3,
@@ -502,10 +487,6 @@ def main():
                     help="untimed FP64 solves before the timed ones (default 1, 0 for C4: ~85 s each)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--ref-budget", type=float, default=15.0)
-    # the reference GMRES (the oracle's restatement, reference arithmetic) reaches
-    # its 1e-6 log on the C2 workload in 5 iterations: 6 preconditioner applies
-    ap.add_argument("--ref-iterations", type=int, default=5)
     ap.add_argument("--apply-only", action="store_true", help="only preconditioner applies (profiling workload)")
     ap.add_argument("--serve", action="store_true", help="serving stream at the rates of --serve-rates")
     ap.add_argument("--serve-rates", default="1,4,16")

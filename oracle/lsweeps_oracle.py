@@ -388,8 +388,13 @@ class DDCheckerboard:
     """Single-process restatement: cell index i*N+j has row I=i, column J=j
     (DDCheckerboard.cpp:185-205 with nprocs = 1)."""
 
-    def setup(self, assembler: AssemblerHelmholtz2DFD, domain, n_cells, n_els_in_cell, verbose=False):
-        """DDCheckerboard::setUp (src/DDCheckerboard.cpp:87-645)."""
+    def setup(self, assembler: AssemblerHelmholtz2DFD, domain, n_cells, n_els_in_cell, verbose=False,
+              assemble=True):
+        """DDCheckerboard::setUp (src/DDCheckerboard.cpp:87-645).  ``assemble``
+        (True, False or a predicate of (I, J)) selects the cells whose matrices
+        and coupling slices are assembled; the others get their geometry and
+        index sets only (a process that owns some cells, as a rank of the
+        reference owns its rows)."""
         order = assembler.order
         tt = int(math.ceil(order / 2.0))
         if n_els_in_cell[0] <= 4 * tt or n_els_in_cell[1] <= 4 * tt:
@@ -452,7 +457,8 @@ class DDCheckerboard:
                 if I == n_cells[0] - 1:
                     l2[5:10] = maxy + h2
                 cell.set_limits(l1, l2)
-                cell.assemble_system_matrix()
+                if assemble is True or (callable(assemble) and assemble(I, J)):
+                    cell.assemble_system_matrix()
                 self.cells.append(cell)
                 if verbose:
                     print("set up", I, "/", J)
@@ -529,27 +535,28 @@ class DDCheckerboard:
 
     def apply_precond(self, x):
         """applyPrecond (DDCheckerboard.cpp:687-739)."""
-        rhs1 = self.get_separated_rhs(x, False, False)
-        rhs2 = self.get_separated_rhs(x, True, False)
-        rhs3 = self.get_separated_rhs(x, False, True)
-        rhs4 = self.get_separated_rhs(x, True, True)
-        r = self.reduce(rhs1)
-        res1 = self.apply_sweep(r, False, False)
-        r = self.reduce(rhs2)
-        r = self.convert_nonshifted_to_shifted_lr(r, False)
-        res2 = self.apply_sweep(r, True, False)
-        res2 = self.convert_shifted_to_nonshifted_lr(res2, False)
-        r = self.reduce(rhs3)
-        r = self.convert_nonshifted_to_shifted_ud(r, False)
-        res3 = self.apply_sweep(r, False, True)
-        res3 = self.convert_shifted_to_nonshifted_ud(res3, False)
-        r = self.reduce(rhs4)
+        res1, res2, res3, res4 = (self.apply_precond_part(x, q) for q in range(4))
+        return [res1[i] + (res2[i] + res3[i] + res4[i]) for i in range(len(self.cells))]
+
+    def apply_precond_part(self, x, q):
+        """The q-th of the four shifted decompositions of applyPrecond
+        (DDCheckerboard.cpp:687-739): q = 0 non-shifted, 1 shifted left-right,
+        2 shifted up-down, 3 shifted both; window, conversion to the shifted
+        ownership, sweep, conversion back."""
+        slr, sud = bool(q & 1), bool(q & 2)
+        r = self.reduce(self.get_separated_rhs(x, slr, sud))
+        if q == 0:
+            return self.apply_sweep(r, False, False)
+        if q == 1:
+            r = self.convert_nonshifted_to_shifted_lr(r, False)
+            return self.convert_shifted_to_nonshifted_lr(self.apply_sweep(r, True, False), False)
+        if q == 2:
+            r = self.convert_nonshifted_to_shifted_ud(r, False)
+            return self.convert_shifted_to_nonshifted_ud(self.apply_sweep(r, False, True), False)
         r = self.convert_nonshifted_to_shifted_lr(r, False)
         r = self.convert_nonshifted_to_shifted_ud(r, True)
-        res4 = self.apply_sweep(r, True, True)
-        res4 = self.convert_shifted_to_nonshifted_ud(res4, True)
-        res4 = self.convert_shifted_to_nonshifted_lr(res4, False)
-        return [res1[i] + (res2[i] + res3[i] + res4[i]) for i in range(len(self.cells))]
+        res = self.convert_shifted_to_nonshifted_ud(self.apply_sweep(r, True, True), True)
+        return self.convert_shifted_to_nonshifted_lr(res, False)
 
     def apply_sweep(self, x, slr, sud):
         """applySweep (DDCheckerboard.cpp:812-880)."""
@@ -576,139 +583,136 @@ class DDCheckerboard:
         d = [key(c.I, c.J) for c in self.cells]
         return sorted(range(len(self.cells)), key=lambda i: (d[i], i))
 
+    def _fronts(self, key):
+        """The cells of _order(key) grouped by equal key: one group is one step of
+        the reference's pipelined sweep (cells on one anti-diagonal, whose solves
+        depend only on groups before it), in the same order."""
+        d = [key(c.I, c.J) for c in self.cells]
+        groups = []
+        for i in self._order(key):
+            if groups and d[groups[-1][0]] == d[i]:
+                groups[-1].append(i)
+            else:
+                groups.append([i])
+        return groups
+
+    def solve_many(self, jobs):
+        """Local solves of one sweep front: jobs = [(cell index, rhs)], returns
+        the solutions in order.  Serial here; a process-parallel executor
+        replaces it (the solves of a front are independent)."""
+        return [self.cells[i].solve(r) for i, r in jobs]
+
+    def matvec_many(self, jobs):
+        """Cell operator products [(cell index, x)] -> [A_cell x] (serial here)."""
+        return [self.cells[i].A @ x for i, x in jobs]
+
     def add_loc_sol(self, x, res, slr, sud):
         """addLocSol (DDCheckerboard.cpp:883-973)."""
         tLR, tUD = [None] * len(self.cells), [None] * len(self.cells)
+        sols = self.solve_many([(i, x[i]) for i in range(len(self.cells))])
         for i, c in enumerate(self.cells):
-            sol = c.solve(x[i])
+            sol = sols[i]
             res[i] += sol
             tUD[i] = self._traces(sol, c.get_index_sets("UpDown", sud))
             tLR[i] = self._traces(sol, c.get_index_sets("LeftRight", slr))
         return tLR, tUD
 
-    def add_left_sweep(self, res, tLR, slr, sud):
-        """addLeftSweep (DDCheckerboard.cpp:976-1164)."""
-        N1, N2 = self.N1, self.N2
-        tmp = [list(t) for t in tLR]
-        tUD = [None] * len(self.cells)
-        for idx in self._order(lambda I, J: (N1 - 1 - I) + (N2 - 1 - J)):
-            c = self.cells[idx]
-            s1, s2 = c.get_index_sets("LeftRight", slr), c.get_index_sets("UpDown", sud)
-            tUD[idx] = [np.zeros(s2[k].size, dtype=np.complex128) for k in (1, 2, 4, 5)]
-            if c.J < N2 - 1:
-                p1 = self.loc(c.I, c.J + 1)
-                tmp[idx][2] = tmp[p1][0]
-                tmp[idx][3] = tmp[p1][1]
-                eq = c.get_equivalent_sources("Right", slr, sud, tmp[idx][3], tmp[idx][2])
+    def _dir_sweep(self, res, tin, slr, sud, order_key, active, nb, trace_type, rows_in, out_dir, own_sets, ins):
+        """One directional sweep (addLeft/Right/Up/DownSweep) front by front: for
+        each cell, the neighbour's outgoing pair becomes this cell's incoming
+        pair, its equivalent sources are solved, the solution is added to res,
+        its cross-direction traces recorded and its outgoing pair accumulated.
+        ins: the (in0, in1) slots of tmp taken from the neighbour's (out0, out1)
+        slots and the order of the trace values given to getEquivalentSources."""
+        tmp = [list(t) for t in tin]
+        tout = [None] * len(self.cells)
+        (i0, i1), (o0, o1), eq_args = ins
+        for group in self._fronts(order_key):
+            jobs, meta = [], []
+            for idx in group:
+                c = self.cells[idx]
+                s1, s2 = c.get_index_sets("LeftRight", slr), c.get_index_sets("UpDown", sud)
+                so = s1 if out_dir == "LR" else s2        # sets of the cross-direction traces
+                si = s1 if out_dir == "UD" else s2        # sets along the sweep direction
+                tout[idx] = [np.zeros(so[k].size, dtype=np.complex128) for k in (1, 2, 4, 5)]
+                if not active(c):
+                    continue
+                p = nb(c)
+                tmp[idx][i0] = tmp[p][o0]
+                tmp[idx][i1] = tmp[p][o1]
+                eq = c.get_equivalent_sources(trace_type, slr, sud, tmp[idx][eq_args[0]], tmp[idx][eq_args[1]])
                 rhs = np.zeros(c.size, dtype=np.complex128)
-                rhs[s1[4]] = eq[1]
-                rhs[s1[5]] = eq[0]
-                sol = c.solve(rhs)
+                rhs[si[rows_in[0]]] = eq[rows_in[2]]
+                rhs[si[rows_in[1]]] = eq[rows_in[3]]
+                jobs.append((idx, rhs))
+                meta.append((so, si))
+            for (idx, _), sol, (so, si) in zip(jobs, self.solve_many(jobs), meta):
                 res[idx] += sol
                 for t, k in zip(range(4), (1, 2, 4, 5)):
-                    tUD[idx][t] = tUD[idx][t] + sol[s2[k]]
-                tmp[idx][0] = tmp[idx][0] + sol[s1[1]]
-                tmp[idx][1] = tmp[idx][1] + sol[s1[2]]
-        return tUD
+                    tout[idx][t] = tout[idx][t] + sol[so[k]]
+                tmp[idx][own_sets[0][0]] = tmp[idx][own_sets[0][0]] + sol[si[own_sets[0][1]]]
+                tmp[idx][own_sets[1][0]] = tmp[idx][own_sets[1][0]] + sol[si[own_sets[1][1]]]
+        return tout
+
+    def add_left_sweep(self, res, tLR, slr, sud):
+        """addLeftSweep (DDCheckerboard.cpp:976-1164): from the right neighbour's
+        (trace0, trace1) as this cell's (traceN, traceNP); sources on traceN /
+        traceNP rows; accumulates trace0 / trace1."""
+        N1, N2 = self.N1, self.N2
+        return self._dir_sweep(res, tLR, slr, sud, lambda I, J: (N1 - 1 - I) + (N2 - 1 - J),
+                               lambda c: c.J < N2 - 1, lambda c: self.loc(c.I, c.J + 1), "Right",
+                               (4, 5, 1, 0), "UD", ((0, 1), (1, 2)), ((2, 3), (0, 1), (3, 2)))
 
     def add_right_sweep(self, res, tLR, slr, sud):
-        """addRightSweep (DDCheckerboard.cpp:1168-1350)."""
-        tmp = [list(t) for t in tLR]
-        tUD = [None] * len(self.cells)
-        for idx in self._order(lambda I, J: I + J):
-            c = self.cells[idx]
-            s1, s2 = c.get_index_sets("LeftRight", slr), c.get_index_sets("UpDown", sud)
-            tUD[idx] = [np.zeros(s2[k].size, dtype=np.complex128) for k in (1, 2, 4, 5)]
-            if c.J > 0:
-                m1 = self.loc(c.I, c.J - 1)
-                tmp[idx][0] = tmp[m1][2]
-                tmp[idx][1] = tmp[m1][3]
-                eq = c.get_equivalent_sources("Left", slr, sud, tmp[idx][0], tmp[idx][1])
-                rhs = np.zeros(c.size, dtype=np.complex128)
-                rhs[s1[1]] = eq[0]
-                rhs[s1[2]] = eq[1]
-                sol = c.solve(rhs)
-                res[idx] += sol
-                for t, k in zip(range(4), (1, 2, 4, 5)):
-                    tUD[idx][t] = tUD[idx][t] + sol[s2[k]]
-                tmp[idx][2] = tmp[idx][2] + sol[s1[4]]
-                tmp[idx][3] = tmp[idx][3] + sol[s1[5]]
-        return tUD
+        """addRightSweep (DDCheckerboard.cpp:1168-1350): from the left neighbour's
+        (traceN, traceNP) as this cell's (trace0, trace1); accumulates traceN /
+        traceNP."""
+        return self._dir_sweep(res, tLR, slr, sud, lambda I, J: I + J,
+                               lambda c: c.J > 0, lambda c: self.loc(c.I, c.J - 1), "Left",
+                               (1, 2, 0, 1), "UD", ((2, 4), (3, 5)), ((0, 1), (2, 3), (0, 1)))
 
     def add_down_sweep(self, res, tUD, slr, sud):
         """addDownSweep (DDCheckerboard.cpp:1353-1540)."""
         N1, N2 = self.N1, self.N2
-        tmp = [list(t) for t in tUD]
-        tLR = [None] * len(self.cells)
-        for idx in self._order(lambda I, J: (N1 - 1 - I) + (N2 - 1 - J)):
-            c = self.cells[idx]
-            s1, s2 = c.get_index_sets("LeftRight", slr), c.get_index_sets("UpDown", sud)
-            tLR[idx] = [np.zeros(s1[k].size, dtype=np.complex128) for k in (1, 2, 4, 5)]
-            if c.I < N1 - 1:
-                p1 = self.loc(c.I + 1, c.J)
-                tmp[idx][2] = tmp[p1][0]
-                tmp[idx][3] = tmp[p1][1]
-                eq = c.get_equivalent_sources("Top", slr, sud, tmp[idx][3], tmp[idx][2])
-                rhs = np.zeros(c.size, dtype=np.complex128)
-                rhs[s2[4]] = eq[1]
-                rhs[s2[5]] = eq[0]
-                sol = c.solve(rhs)
-                res[idx] += sol
-                for t, k in zip(range(4), (1, 2, 4, 5)):
-                    tLR[idx][t] = tLR[idx][t] + sol[s1[k]]
-                tmp[idx][0] = tmp[idx][0] + sol[s2[1]]
-                tmp[idx][1] = tmp[idx][1] + sol[s2[2]]
-        return tLR
+        return self._dir_sweep(res, tUD, slr, sud, lambda I, J: (N1 - 1 - I) + (N2 - 1 - J),
+                               lambda c: c.I < N1 - 1, lambda c: self.loc(c.I + 1, c.J), "Top",
+                               (4, 5, 1, 0), "LR", ((0, 1), (1, 2)), ((2, 3), (0, 1), (3, 2)))
 
     def add_up_sweep(self, res, tUD, slr, sud):
         """addUpSweep (DDCheckerboard.cpp:1544-1724)."""
-        tmp = [list(t) for t in tUD]
-        tLR = [None] * len(self.cells)
-        for idx in self._order(lambda I, J: I + J):
-            c = self.cells[idx]
-            s1, s2 = c.get_index_sets("LeftRight", slr), c.get_index_sets("UpDown", sud)
-            tLR[idx] = [np.zeros(s1[k].size, dtype=np.complex128) for k in (1, 2, 4, 5)]
-            if c.I > 0:
-                m1 = self.loc(c.I - 1, c.J)
-                tmp[idx][0] = tmp[m1][2]
-                tmp[idx][1] = tmp[m1][3]
-                eq = c.get_equivalent_sources("Bottom", slr, sud, tmp[idx][0], tmp[idx][1])
-                rhs = np.zeros(c.size, dtype=np.complex128)
-                rhs[s2[1]] = eq[0]
-                rhs[s2[2]] = eq[1]
-                sol = c.solve(rhs)
-                res[idx] += sol
-                for t, k in zip(range(4), (1, 2, 4, 5)):
-                    tLR[idx][t] = tLR[idx][t] + sol[s1[k]]
-                tmp[idx][2] = tmp[idx][2] + sol[s2[4]]
-                tmp[idx][3] = tmp[idx][3] + sol[s2[5]]
-        return tLR
+        return self._dir_sweep(res, tUD, slr, sud, lambda I, J: I + J,
+                               lambda c: c.I > 0, lambda c: self.loc(c.I - 1, c.J), "Bottom",
+                               (1, 2, 0, 1), "LR", ((2, 4), (3, 5)), ((0, 1), (2, 3), (0, 1)))
 
     def _lsweep(self, res, tLR, tUD, slr, sud, lt, order_key, active, pull, extract_args,
                 overwrite, overwrite_before_add, push):
         tLR = [list(t) for t in tLR]
         tUD = [list(t) for t in tUD]
-        for idx in self._order(order_key):
-            c = self.cells[idx]
-            if not active(c.I, c.J):
-                continue
-            s1, s2 = c.get_index_sets("LeftRight", slr), c.get_index_sets("UpDown", sud)
-            pull(idx, c, tLR, tUD)
-            lr0, lr1, ud0, ud1 = extract_args(idx, tLR, tUD)
-            lv = c.extract_ltraces(lt, slr, sud, lr0, lr1, ud0, ud1)
-            eq = c.get_equivalent_sources(lt, slr, sud, lv[0], lv[1])
-            l0, l1 = c.ltr[(lt, slr, sud)]
-            rhs = np.zeros(c.size, dtype=np.complex128)
-            rhs[l0] = eq[0]
-            rhs[l1] = eq[1]
-            sol = c.solve(rhs)
-            if overwrite_before_add:
-                overwrite(idx, sol, s1, s2, tLR, tUD)
-                res[idx] += sol
-            else:
-                res[idx] += sol
-                overwrite(idx, sol, s1, s2, tLR, tUD)
-            push(idx, sol, s1, s2, tLR, tUD)
+        for group in self._fronts(order_key):
+            jobs = []
+            for idx in group:
+                c = self.cells[idx]
+                if not active(c.I, c.J):
+                    continue
+                pull(idx, c, tLR, tUD)
+                lr0, lr1, ud0, ud1 = extract_args(idx, tLR, tUD)
+                lv = c.extract_ltraces(lt, slr, sud, lr0, lr1, ud0, ud1)
+                eq = c.get_equivalent_sources(lt, slr, sud, lv[0], lv[1])
+                l0, l1 = c.ltr[(lt, slr, sud)]
+                rhs = np.zeros(c.size, dtype=np.complex128)
+                rhs[l0] = eq[0]
+                rhs[l1] = eq[1]
+                jobs.append((idx, rhs))
+            for (idx, _), sol in zip(jobs, self.solve_many(jobs)):
+                c = self.cells[idx]
+                s1, s2 = c.get_index_sets("LeftRight", slr), c.get_index_sets("UpDown", sud)
+                if overwrite_before_add:
+                    overwrite(idx, sol, s1, s2, tLR, tUD)
+                    res[idx] += sol
+                else:
+                    res[idx] += sol
+                    overwrite(idx, sol, s1, s2, tLR, tUD)
+                push(idx, sol, s1, s2, tLR, tUD)
 
     def add_bl2tr_sweep(self, res, tLR, tUD, slr, sud):
         """addBL2TRSweep (DDCheckerboard.cpp:2393-2608); overwrites trace0 entries
@@ -868,7 +872,7 @@ class DDCheckerboard:
             if c.I < self.N1 - 1:
                 p = self.cells[self.loc(c.I + 1, c.J)]
                 xe[idx][s2[5]] = xe[self.loc(c.I + 1, c.J)][p.get_index_sets("UpDown", False)[2]]
-        return self.reduce([self.cells[i].A @ xe[i] for i in range(len(self.cells))])
+        return self.reduce(self.matvec_many([(i, xe[i]) for i in range(len(self.cells))]))
 
 
 # ----------------------------------------------------------------------------

@@ -10,7 +10,7 @@ ROOT = Path(__file__).resolve().parent.parent
 
 def test_reference_arm_prints_a_contract_line():
     r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1",
-                        "--warmup", "1", "--ref-budget", "2"], capture_output=True, text=True, timeout=600,
+                        "--warmup", "1", "--config", "C1"], capture_output=True, text=True, timeout=600,
                        cwd=str(ROOT))
     assert r.returncode == 0, r.stderr[-2000:]
     line = json.loads(r.stdout.strip().splitlines()[-1])

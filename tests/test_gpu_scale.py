@@ -1,0 +1,96 @@
+"""Parity at the benchmark sizes (through the C ABI, on the GPU).
+
+* C2 (1031^2, 64 cells): the CUDA preconditioner against the oracle's apply
+  (process-parallel executor, every host core) on one random vector --
+  complex128 <= 1e-10, complex64 and bf16 split <= 2e-4; and the reference-
+  mode GMRES (complex128) against the oracle's restatement of
+  GlobalIterativeSolverGMRES::solve: iteration count within +-1, residual log
+  within 1e-6 relative.
+* C2 and C4 (4127^2, 1024 cells): the mixed-precision FGMRES solutions
+  (complex64 and bf16 split factors) within 1e-5 of the FP64 GPU solution,
+  every true relative residual <= 1e-6.
+The committed reference-GMRES iteration counts used by the CPU baseline
+(tests/golden/reference_gmres_iterations.json) are checked at C2 as well."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from lsweeps.problems import config  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _solver(spec, med, prec):
+    from lsweeps.solver import Solver
+    S = Solver(spec, med, precision=prec)
+    S.factorize()
+    return S
+
+
+@pytest.fixture(scope="module")
+def c2():
+    from oracle.parallel import ParallelOracle
+    spec, med = config("C2")
+    with ParallelOracle(spec.N, spec.m, spec.p, spec.h, spec.omega, med) as Q:
+        yield spec, med, Q
+
+
+def test_c2_precond_matches_oracle(c2):
+    spec, med, Q = c2
+    rng = np.random.default_rng(2)
+    n2 = Q.n_dof ** 2
+    v = rng.standard_normal(n2) + 1j * rng.standard_normal(n2)
+    y_or = Q.apply_precond_global(v)
+    for prec, tol in (("c128", 1e-10), ("c64", 2e-4), ("bf16x2", 2e-4)):
+        S = _solver(spec, med, prec)
+        y = S.apply_precond(torch.from_numpy(v).cuda()).cpu().numpy()
+        S.close()
+        assert rel(y, y_or) <= tol, prec
+
+
+def test_c2_reference_gmres_matches_oracle(c2):
+    from oracle.lsweeps_oracle import gmres_reference
+    spec, med, Q = c2
+    S = _solver(spec, med, "c128")
+    b = S.assemble_rhs(spec.sources)
+    x, rep = S.gmres(b, mode="reference", tol=1e-6, max_iter=40)
+    xo, ro = gmres_reference(Q.dd, Q.cells_of(b.cpu().numpy()), tol=1e-6, max_iter=40)
+    S.close()
+    assert abs(rep.iterations - ro.iterations) <= 1
+    n = min(len(rep.log), len(ro.log))
+    assert np.allclose(rep.log[:n], ro.log[:n], rtol=1e-6, atol=1e-12)
+    fixture = json.loads((GOLDEN / "reference_gmres_iterations.json").read_text())
+    assert abs(fixture["C2"]["iterations"] - ro.iterations) <= 1
+    if rep.iterations == ro.iterations:
+        assert rel(x.cpu().numpy(), Q.global_of(xo)) <= 1e-8
+
+
+@pytest.mark.parametrize("name,mixed", [("C2", ("c64", "bf16x2")), ("C4", ("bf16x2", "c64"))])
+def test_mixed_precision_matches_fp64_at_scale(name, mixed):
+    spec, med = config(name)
+    S = _solver(spec, med, "c128")
+    b = S.assemble_rhs(spec.sources)
+    x64, r64 = S.gmres(b, mode="flexible", tol=1e-6, max_iter=300, restart=30)
+    assert r64.converged and r64.true_rel_res <= 1e-6
+    x64h = x64.cpu().numpy()
+    S.close()
+    del x64
+    torch.cuda.empty_cache()
+    for prec in mixed:
+        S = _solver(spec, med, prec)
+        x, r = S.gmres(b, mode="flexible", tol=1e-6, max_iter=300, restart=30)
+        assert r.converged and r.true_rel_res <= 1e-6, prec
+        assert rel(x.cpu().numpy(), x64h) <= 1e-5, prec
+        assert abs(r.iterations - r64.iterations) <= 2, prec
+        S.close()
+        del x
+        torch.cuda.empty_cache()
