@@ -149,6 +149,15 @@ lsw_status lsw_ctx_destroy(lsw_ctx* ctx);
 const char* lsw_status_string(lsw_status s);
 const char* lsw_ctx_last_error(const lsw_ctx* ctx);
 
+/* Replay each preconditioner apply as a CUDA graph (enable = 1, the default;
+ * LSW_GRAPHS=0 in the environment at context creation turns it off) or launch
+ * its kernels one by one (enable = 0).  One graph per batch size is captured
+ * on first use and captured again when the context's sweep pools are
+ * reallocated or released; both ways run the same kernels on the same data and
+ * give identical results.  No counterpart in the reference (its applies are
+ * host loops over MPI ranks, DDCheckerboard.cpp:687-739). */
+lsw_status lsw_ctx_set_graphs(lsw_ctx* ctx, int enable);
+
 /* Limit of every bounded wait inside the context's kernels (default ~2 s).
  * A wait that runs out makes its kernel give up and return normally; the call
  * that launched it then returns LSW_ERR_CUDA (results invalid).  No

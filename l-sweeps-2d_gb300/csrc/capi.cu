@@ -71,6 +71,8 @@ struct lsw_ctx {
   int max_cluster = 8;
   int krylov_batch = 0;   // right-hand sides per Krylov sub-batch at most (0: as memory allows)
   bool factor_lookahead = true;
+  // complex64 / split factorisation on the tensor cores (else the CUDA-core kernel)
+  bool factor_tc = true;
   // bounded-wait limit of the sweep and factorisation kernels, in SM clock cycles
   long long wait_cycles = 4000000000LL;   // ~2 s at 2 GHz
   // device address of the allocation-free solve's fixed scratch array on this
@@ -78,6 +80,29 @@ struct lsw_ctx {
   void* noalloc_base = nullptr;
   // optional per-front timing of one apply
   std::vector<cudaEvent_t>* front_events = nullptr;
+  // CUDA graphs of the apply, one per batch size, replayed on the caller's
+  // stream; a graph is captured against the pools of generation `gen` and
+  // captured again when a pool it uses has been reallocated or released
+  struct ApplyGraph {
+    cudaGraphExec_t exec = nullptr;
+    long long gen = -1;
+    int kernels = 0;
+  };
+  std::map<int, ApplyGraph> graphs;
+  bool use_graphs = true;
+  long long pool_gen = 0;
+  cudaStream_t cap_stream = nullptr;
+  DevBuf d_ref;   // the captured applies' address table: input, output
+  void drop_graphs() {
+    for (auto& kv : graphs)
+      if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    graphs.clear();
+    ++pool_gen;
+  }
+  ~lsw_ctx() {
+    drop_graphs();
+    if (cap_stream) cudaStreamDestroy(cap_stream);
+  }
 };
 
 namespace {
@@ -152,7 +177,7 @@ size_t device_bytes(const lsw_ctx* c) {
              c->d_work.bytes + c->d_status.bytes + c->d_traces.bytes + c->d_outs.bytes + c->d_scratch.bytes +
              c->k_basis.bytes + c->k_zbasis.bytes + c->k_tmp.bytes + c->k_tmp2.bytes + c->k_r.bytes +
              c->k_part.bytes + c->k_small.bytes + c->k_small2.bytes + c->k_nrm.bytes + c->ls_items.bytes +
-             c->ls_slots.bytes + c->ls_scratch.bytes + c->h_b.bytes + c->h_x.bytes;
+             c->ls_slots.bytes + c->ls_scratch.bytes + c->h_b.bytes + c->h_x.bytes + c->d_ref.bytes;
   for (auto& kv : c->sched_bufs)
     for (int i = 0; i < 3; ++i) b += kv.second[i].bytes;
   return b;
@@ -209,17 +234,27 @@ lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out) {
   }
   Schedule* sc = it->second.get();
   const size_t cs = csize(ctx->prec);
+  void* const before[3] = {ctx->d_traces.p, ctx->d_outs.p, ctx->d_scratch.p};
   CK(ctx->d_traces.ensure((size_t)nrhs * 4 * ctx->ncell * 24 * ctx->LP * cs), "cudaMalloc(traces)");
   CK(ctx->d_outs.ensure((size_t)nrhs * 4 * ctx->n2 * cs), "cudaMalloc(outs)");
   CK(ctx->d_scratch.ensure(std::max<size_t>(1, (size_t)sc->scratch_elems * cs)), "cudaMalloc(scratch)");
+  if (before[0] != ctx->d_traces.p || before[1] != ctx->d_outs.p || before[2] != ctx->d_scratch.p) {
+    // the captured applies point at the old pools
+    for (auto& kv : ctx->graphs)
+      if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    ctx->graphs.clear();
+    ++ctx->pool_gen;
+  }
   *out = sc;
   return LSW_OK;
 }
 
-lsw_status precond_impl(lsw_ctx* ctx, const double2* x, double2* y, int nrhs, cudaStream_t st) {
-  Schedule* sc = nullptr;
-  lsw_status s = ensure_batch(ctx, nrhs, &sc);
-  if (s != LSW_OK) return s;
+// The launches of one apply on stream st: clear the trace and output pools,
+// every sweep front, the sum of the four shifted outputs.  The input and
+// output addresses are read from ctx->d_ref (set by the caller beforehand),
+// so the sequence can be captured once and replayed for any vectors.
+// Returns the number of kernels enqueued in *kernels.
+lsw_status enqueue_apply(lsw_ctx* ctx, Schedule* sc, int nrhs, cudaStream_t st, int* kernels) {
   const size_t cs = csize(ctx->prec);
   CK(cudaMemsetAsync(ctx->d_traces.p, 0, (size_t)nrhs * 4 * ctx->ncell * 24 * ctx->LP * cs, st), "memset traces");
   CK(cudaMemsetAsync(ctx->d_outs.p, 0, (size_t)nrhs * 4 * ctx->n2 * cs, st), "memset outs");
@@ -232,12 +267,14 @@ lsw_status precond_impl(lsw_ctx* ctx, const double2* x, double2* y, int nrhs, cu
   a.traces = ctx->d_traces.p;
   a.outs = ctx->d_outs.p;
   a.scratch = ctx->d_scratch.p;
-  a.x_in = x;
+  a.x_in = nullptr;
+  a.x_ref = reinterpret_cast<const double2* const*>(ctx->d_ref.p);
   a.x_stride = ctx->n2;
   a.n_dof = ctx->n_dof; a.N = ctx->N; a.m = ctx->m; a.p = ctx->p;
   a.err = ctx->d_status.as<int>() + 1;
   a.wait_cycles = ctx->wait_cycles;
   a.split = ctx->prec == LSW_PREC_SPLIT ? 1 : 0;
+  int k = 0;
   for (size_t fi = 0; fi < sc->fronts.size(); ++fi) {
     const Front& f = sc->fronts[fi];
     a.items = sc->d_items + f.item_begin;
@@ -249,12 +286,51 @@ lsw_status precond_impl(lsw_ctx* ctx, const double2* x, double2* y, int nrhs, cu
                                                : launch_front<double>(a, ctx->max_ny, ctx->max_nx, st);
     CK(e, "front kernel");
     if (ctx->front_events) CK(cudaEventRecord((*ctx->front_events)[2 * fi + 1], st), "event");
-    ctx->launches += f.item_count > 0 ? 1 : 0;
+    k += f.item_count > 0 ? 1 : 0;
   }
-  ctx->launches += 1;
-  cudaError_t e = ctx->prec != LSW_PREC_C128 ? launch_combine<float>(ctx->d_outs.p, y, nrhs, ctx->n2, st)
-                                             : launch_combine<double>(ctx->d_outs.p, y, nrhs, ctx->n2, st);
+  double2* const* yref = reinterpret_cast<double2* const*>(ctx->d_ref.p) + 1;
+  cudaError_t e = ctx->prec != LSW_PREC_C128 ? launch_combine_ref<float>(ctx->d_outs.p, yref, nrhs, ctx->n2, st)
+                                             : launch_combine_ref<double>(ctx->d_outs.p, yref, nrhs, ctx->n2, st);
   CK(e, "combine kernel");
+  *kernels = k + 1;
+  return LSW_OK;
+}
+
+lsw_status precond_impl(lsw_ctx* ctx, const double2* x, double2* y, int nrhs, cudaStream_t st) {
+  Schedule* sc = nullptr;
+  lsw_status s = ensure_batch(ctx, nrhs, &sc);
+  if (s != LSW_OK) return s;
+  CK(ctx->d_ref.ensure(2 * sizeof(void*)), "cudaMalloc(address table)");
+  KL(1, launch_set_refs(reinterpret_cast<const void**>(ctx->d_ref.p), x, y, st), "address table");
+  int kernels = 0;
+  if (!ctx->use_graphs || ctx->front_events) {
+    s = enqueue_apply(ctx, sc, nrhs, st, &kernels);
+    ctx->launches += kernels;
+    return s;
+  }
+  lsw_ctx::ApplyGraph& g = ctx->graphs[nrhs];
+  if (!g.exec || g.gen != ctx->pool_gen) {
+    if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
+    if (!ctx->cap_stream) CK(cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking), "capture stream");
+    CK(cudaStreamBeginCapture(ctx->cap_stream, cudaStreamCaptureModeRelaxed), "begin capture");
+    s = enqueue_apply(ctx, sc, nrhs, ctx->cap_stream, &kernels);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(ctx->cap_stream, &graph);
+    if (s != LSW_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return s;
+    }
+    CK(e, "end capture");
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(ei, "graph instantiate");
+    g.exec = exec;
+    g.gen = ctx->pool_gen;
+    g.kernels = kernels;
+  }
+  CK(cudaGraphLaunch(g.exec, st), "graph launch");
+  ctx->launches += g.kernels;
   return LSW_OK;
 }
 
@@ -394,6 +470,10 @@ lsw_status lsw_ctx_create(lsw_ctx** out, int device) {
   if (const char* ev = std::getenv("LSW_KRYLOV_BATCH")) c->krylov_batch = std::max(0, std::atoi(ev));
   // LSW_FACTOR_LOOKAHEAD=0 factors each panel after the whole previous update
   if (const char* ev = std::getenv("LSW_FACTOR_LOOKAHEAD")) c->factor_lookahead = std::atoi(ev) != 0;
+  // LSW_GRAPHS=0 launches every apply's kernels one by one instead of replaying a CUDA graph
+  if (const char* ev = std::getenv("LSW_GRAPHS")) c->use_graphs = std::atoi(ev) != 0;
+  // LSW_FACTOR_TC=0 runs the complex64 / split factorisation on the CUDA cores
+  if (const char* ev = std::getenv("LSW_FACTOR_TC")) c->factor_tc = std::atoi(ev) != 0;
   // the host-side name of the allocation-free solve's scratch array is not a
   // device address: look the address up on this device (current since the
   // cudaSetDevice above) and keep it with the context
@@ -403,6 +483,12 @@ lsw_status lsw_ctx_create(lsw_ctx** out, int device) {
     return LSW_ERR_CUDA;
   }
   *out = c;
+  return LSW_OK;
+}
+
+lsw_status lsw_ctx_set_graphs(lsw_ctx* ctx, int enable) {
+  if (!ctx) return LSW_ERR_INVALID_ARGUMENT;
+  ctx->use_graphs = enable != 0;
   return LSW_OK;
 }
 
@@ -452,6 +538,7 @@ lsw_status lsw_problem_setup(lsw_ctx* ctx, const lsw_geom* g, const double* m_gr
     return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "unknown precision");
   CK(cudaSetDevice(ctx->device), "cudaSetDevice");
   // drop everything of a previous problem
+  ctx->drop_graphs();
   ctx->sched.clear(); ctx->sched_bufs.clear();
   ctx->is_setup = false; ctx->factorized = false;
   ctx->geom = *g;
@@ -534,7 +621,12 @@ lsw_status lsw_factorize(lsw_ctx* ctx, void* stream) {
   CK(cudaMemsetAsync(ctx->d_status.p, 0, 16, st), "memset status");
   ctx->launches += 2;   // half chains, middle lines
   const double w2 = ctx->omega * ctx->omega;
-  cudaError_t e = ctx->prec != LSW_PREC_C128
+  const bool tc = ctx->prec != LSW_PREC_C128 && ctx->factor_tc && factorize_tc_supported(ctx->max_ny);
+  cudaError_t e = tc ? launch_factorize_tc(ctx->d_cells.as<DevCell>(), ctx->ncell, ctx->d_prof.as<double2>(),
+                                           ctx->d_m.as<double>(), ctx->n_dof, w2, ctx->d_fac.p, ctx->d_work.p,
+                                           ctx->max_ny, ctx->d_status.as<int>(), st, ctx->prec == LSW_PREC_SPLIT,
+                                           ctx->wait_cycles)
+                  : ctx->prec != LSW_PREC_C128
                       ? launch_factorize<float>(ctx->d_cells.as<DevCell>(), ctx->ncell, ctx->d_prof.as<double2>(),
                                                 ctx->d_m.as<double>(), ctx->n_dof, w2, ctx->d_fac.p, ctx->d_work.p,
                                                 ctx->max_ny, ctx->d_status.as<int>(), st, ctx->prec == LSW_PREC_SPLIT,
@@ -1114,6 +1206,7 @@ lsw_status lsw_release_workspace(lsw_ctx* ctx) {
   if (!ctx) return LSW_ERR_INVALID_ARGUMENT;
   CK(cudaSetDevice(ctx->device), "cudaSetDevice");
   CK(cudaDeviceSynchronize(), "sync");   // no launch may still use the buffers
+  ctx->drop_graphs();
   ctx->sched.clear();
   ctx->sched_bufs.clear();
   for (DevBuf* b : {&ctx->d_traces, &ctx->d_outs, &ctx->d_scratch, &ctx->k_basis, &ctx->k_zbasis, &ctx->k_tmp,

@@ -269,9 +269,12 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
   }
 
   // ---- flatten into items ----
-  // An item takes whole (rhs, shift) groups while they fit in r slots; a
-  // group larger than r is split over items (its outputs are added
-  // atomically, so the split only costs an extra read of the factor).
+  // An item takes whole (rhs, shift) groups while they fit in r slots.  A
+  // group holds at most 4 slots (the four sweep directions, or the four
+  // L-sweeps, that reach one cell in one front), and the planner only tries
+  // r >= 4, so no group is split over items: every owned output value and
+  // every trace line is written by one item per front, in one order, and the
+  // apply is deterministic (the output adds need no ordering between items).
   auto flatten = [&](std::vector<SlotSpec>& v, int r, auto&& emit) {
     size_t i = 0;
     while (i < v.size()) {
@@ -306,7 +309,7 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
     int best_r = plan.rmax, best_cl = 1;
     double best_t = 1e300;
     long long best_items = 0;
-    for (int r : {16, 8, 4, 2, 1}) {
+    for (int r : {16, 8, 4}) {
       if (r > plan.rmax) continue;
       long long n_items = 0;
       int maxs = 0;

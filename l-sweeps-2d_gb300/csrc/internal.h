@@ -152,6 +152,9 @@ struct FrontArgs {
   void* outs;             // out pool (cx_t<T>)
   void* scratch;          // forward storage (cx_t<T>)
   const double2* x_in;    // global input vectors (VOLUME) or cell vectors (CELLVEC)
+  // when set, the VOLUME input is *x_ref (a device-side address table, so that
+  // one captured launch sequence serves any input vector)
+  const double2* const* x_ref;
   long long x_stride;
   double2* x_out;         // CELLVEC output
   long long out_stride;
@@ -193,6 +196,13 @@ template <typename T> cudaError_t launch_factorize(const DevCell* cells, int nce
 // one bounded wait on a barrier that nothing completes (bit 1 of *err when it runs out)
 cudaError_t launch_wait_probe(int* err, long long limit_cycles, cudaStream_t st);
 size_t factor_smem_bytes(int ny, bool dbl);
+// complex64 / split factorisation with the working matrix in tensor memory and
+// each block's update on the tensor cores (3 x TF32 tcgen05.mma); cells of at
+// most 192 DOFs per side
+bool factorize_tc_supported(int max_ny);
+cudaError_t launch_factorize_tc(const DevCell* cells, int ncell, const double2* prof, const double* mgrid, int n_dof,
+                                double omega2, void* fac, void* prev, int max_ny, int* status, cudaStream_t st,
+                                bool split, long long wait_cycles);
 
 cudaError_t launch_apply_A(const double2* x, double2* y, int nrhs, int n_dof, const double2* gprof,
                            const double* mgrid, double omega2, cudaStream_t st);
@@ -200,6 +210,11 @@ template <typename T> cudaError_t launch_combine(const void* outs, double2* y, i
                                                  cudaStream_t st);
 cudaError_t launch_rhs(double2* b, int n_dof, int p, double h, const double* src, const double* amp,
                        int nsrc, double eps, cudaStream_t st);
+// combine into *y_ref (the output address read from device memory)
+template <typename T> cudaError_t launch_combine_ref(const void* outs, double2* const* y_ref, int nrhs, long long n2,
+                                                     cudaStream_t st);
+// ref[0] = x, ref[1] = y (the address table of a captured apply)
+cudaError_t launch_set_refs(const void** ref, const void* x, void* y, cudaStream_t st);
 
 // FP64 Krylov helpers; results of reductions land in device memory.
 cudaError_t launch_dot(const double2* a, const double2* b, long long n, int nvec, long long stride,

@@ -395,6 +395,7 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
 
   const C* tr = reinterpret_cast<const C*>(a.traces);
   C* trw = reinterpret_cast<C*>(a.traces);
+  const double2* x_in = a.x_ref ? *a.x_ref : a.x_in;   // the VOLUME input
   const C* fac = reinterpret_cast<const C*>(a.fac) + cl.fac_off;
   C* scr = reinterpret_cast<C*>(a.scratch) + it.scratch_off;
   C* outs = reinterpret_cast<C*>(a.outs);
@@ -483,7 +484,7 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
         const int sx = sr.shift & 1, sy = (sr.shift >> 1) & 1;
         const int fx = linef[k], fy = colf[jj];
         if (((fx >> (1 + sx)) & 1) && ((fy >> (1 + sy)) & 1) && (fx & 1) == sx && (fy & 1) == sy)
-          v = to_c(a.x_in[(long long)sr.rhs * a.x_stride + (long long)(cl.lox + k) * a.n_dof + cl.loy + j], czero<C>());
+          v = to_c(x_in[(long long)sr.rhs * a.x_stride + (long long)(cl.lox + k) * a.n_dof + cl.loy + j], czero<C>());
       } else if (sr.kind != SK_NONE) {
         v = rhs_elem<T>(a, cl, sr, cf[r], tr, k, j);
       }

@@ -22,7 +22,7 @@ EXPORTS = [
     "lsw_problem_setup", "lsw_problem_info_get", "lsw_cell_info_get", "lsw_factorize", "lsw_apply_precond",
     "lsw_apply_A", "lsw_assemble_rhs", "lsw_gmres", "lsw_solve_host", "lsw_local_solve",
     "lsw_apply_precond_profiled", "lsw_local_solve_noalloc", "lsw_release_workspace",
-    "lsw_ctx_set_wait_limit", "lsw_selftest_bounded_wait",
+    "lsw_ctx_set_wait_limit", "lsw_selftest_bounded_wait", "lsw_ctx_set_graphs",
 ]
 
 
@@ -106,6 +106,7 @@ def lib() -> C.CDLL:
         "lsw_release_workspace": (i, [vp]),
         "lsw_ctx_set_wait_limit": (i, [vp, d]),
         "lsw_selftest_bounded_wait": (i, [vp, vp]),
+        "lsw_ctx_set_graphs": (i, [vp, i]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -163,3 +163,27 @@ def test_driver_reports_input_errors(tmp_path):
     f.write_text('Problems = ( { DomainDecomposition = "CheckerboardDD"; } );')
     r = subprocess.run([str(MAIN), str(f)], capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "DomainDecompositionID" in r.stderr
+
+
+def test_abstract_interface_driver_runs(tmp_path):
+    """A driver written only against the abstract plugin classes (DD,
+    Subdomain, Assembler, PML, LocalLinearSolver, GlobalIterativeSolver,
+    Output; tests/host/abstract_driver.cpp) builds, solves on the GPU, copies
+    its decomposition (DD::copy) and writes the wavefield."""
+    import shutil
+    lib = ROOT / "l-sweeps-2d_gb300" / "lsweeps"
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    exe = tmp_path / "abstract_driver"
+    r = subprocess.run([cxx, "-std=c++17", "-O1", str(ROOT / "tests" / "host" / "abstract_driver.cpp"), "-I",
+                        str(ROOT / "include"), "-L", str(lib), "-llsweeps_gb300", f"-Wl,-rpath,{lib}", "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = tmp_path / "wave"
+    r = subprocess.run([str(exe), str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    vtk = (tmp_path / "wave.vtk").read_text().splitlines()
+    i = vtk.index("SCALARS wavefield_re float")
+    vals = np.array([float(v) for v in vtk[i + 2:i + 2 + 48 * 48]])
+    assert np.isfinite(vals).all() and np.abs(vals).max() > 0
