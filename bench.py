@@ -349,6 +349,36 @@ def run_gpu(args):
         prof_runs.append(pr)
     front_ms = statistics.median(p["front_ms"] for p in prof_runs)
     pr = prof_runs[-1]
+
+    # launch shapes: the tuner's per-front choice against the cost model's, and
+    # one apply replayed as a CUDA graph against its kernels launched one by one
+    def apply_ms(reps=3):
+        ts = []
+        for _ in range(reps + 1):
+            a1, a2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a1.record(st)
+            S.apply_precond(v)
+            a2.record(st)
+            torch.cuda.synchronize()
+            ts.append(a1.elapsed_time(a2))
+        return statistics.median(ts[1:])
+    shapes, tune_s = S.front_shapes(nrhs)
+    t_tuned_graph = apply_ms()
+    S.set_graphs(False)
+    t_tuned_eager = apply_ms()
+    S.set_graphs(True)
+    S.set_tuning(False)
+    t_model_graph = apply_ms()
+    model_shapes, _ = S.front_shapes(nrhs)
+    S.set_tuning(True)
+    apply_ms(1)
+    launch = {
+        "apply_ms_tuned_graph": t_tuned_graph, "apply_ms_tuned_eager": t_tuned_eager,
+        "apply_ms_model_graph": t_model_graph, "tune_s": tune_s,
+        "fronts_changed_by_tuner": sum(1 for a, b in zip(shapes, model_shapes)
+                                       if (a["slots_cap"], a["cluster"]) != (b["slots_cap"], b["cluster"])),
+        "tuned_shapes": " ".join(f"{f['slots_cap']}x{f['cluster']}" for f in shapes),
+    }
     peak, peak_kind = measured_peaks()
     achieved = pr["alg_bytes"] / (front_ms / 1e3) / 1e9
     traffic = None
@@ -420,6 +450,7 @@ def run_gpu(args):
                          "streamed_bytes_per_apply": pr["streamed_bytes"],
                          "front_ms_per_apply": front_ms, "fronts": pr["fronts"], "items": pr["items"],
                          "slots": pr["slots"], "apply_ms": pr["total_ms"]},
+            "launch_shapes": launch,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": S.n2 * 16 * nrhs,
                     "d2h_bytes_per_step": S.n2 * 16 * nrhs, "steps": len(te)},

@@ -26,7 +26,9 @@
  *   - Every call returns an lsw_status instead of exiting the process (the
  *     reference prints to cerr and calls exit(1)).  One context per host thread,
  *     or external locking; the library keeps no global state except the
- *     library-wide status strings.
+ *     library-wide status strings, the sweep-front tuner's cache of measured
+ *     launch shapes (per GPU and problem shape, behind a lock) and the fixed
+ *     scratch array of lsw_local_solve_noalloc.
  */
 #ifndef LSWEEPS_H
 #define LSWEEPS_H
@@ -157,6 +159,38 @@ const char* lsw_ctx_last_error(const lsw_ctx* ctx);
  * give identical results.  No counterpart in the reference (its applies are
  * host loops over MPI ranks, DDCheckerboard.cpp:687-739). */
 lsw_status lsw_ctx_set_graphs(lsw_ctx* ctx, int enable);
+
+/* Sweep-front launch shapes.  Each front (one launch per stage step, every
+ * cell of the step, all four shifted decompositions and every right-hand side)
+ * is cut into items of at most `slots_cap` right-hand-side slots of one cell,
+ * each item a thread-block cluster of 2 x `cluster` CTAs (the two half chains
+ * of the cell's twisted block solve).  With tuning on (enable = 1, the default;
+ * LSW_TUNE=0 in the environment at context creation turns it off) the first
+ * apply of a batch size measures every shape (slots 4, 8, 16 x CTAs 1, 2, 4
+ * per half) on every front where it fits, with CUDA events on the call's
+ * stream, and keeps each front's fastest; the choice is cached per GPU (UUID)
+ * and problem shape for the process, and appended to the file named by
+ * LSW_TUNE_CACHE when that is set (read back by later processes).  With
+ * tuning off a cost model chooses.  Changing the setting drops the context's
+ * schedules (rebuilt on next use; waits for the device).  No counterpart in the
+ * reference (its sweeps are host loops, DDCheckerboard.cpp:812-880). */
+lsw_status lsw_ctx_set_tuning(lsw_ctx* ctx, int enable);
+
+typedef struct {
+  int items;        /* items (cluster launches) in the front */
+  int max_slots;    /* slots of the largest item */
+  int slots_cap;    /* slots per item at most */
+  int cluster;      /* CTAs per half chain */
+  float tuned_ms;   /* the tuner's time for this front's shape; -1 when the cost model chose it */
+} lsw_front_shape;
+
+/* The launch shapes of the sweep fronts of a batch of nrhs right-hand sides
+ * (building, and with tuning on measuring, the schedule if this batch size has
+ * none yet, on `stream`): up to `capacity` entries in `out`, the front count in
+ * *n_fronts, the context's total tuning time so far in *tune_seconds (may be
+ * NULL).  Requires a factorised problem. */
+lsw_status lsw_front_shapes(lsw_ctx* ctx, int nrhs, lsw_front_shape* out, int capacity, int* n_fronts,
+                            double* tune_seconds, void* stream);
 
 /* Limit of every bounded wait inside the context's kernels (default ~2 s).
  * A wait that runs out makes its kernel give up and return normally; the call

@@ -60,7 +60,7 @@ struct lsw_ctx {
   std::map<int, std::unique_ptr<DevBuf[]>> sched_bufs;
   DevBuf d_traces, d_outs, d_scratch;
   // Krylov workspace
-  DevBuf k_basis, k_zbasis, k_tmp, k_tmp2, k_r, k_part, k_small, k_small2, k_nrm;
+  DevBuf k_basis, k_zbasis, k_tmp, k_tmp2, k_r, k_part, k_small, k_small2, k_nrm, k_ls;
   // local-solve workspace
   DevBuf ls_items, ls_slots, ls_scratch;
   // lsw_solve_host's device copies of b and x, kept between calls
@@ -72,7 +72,11 @@ struct lsw_ctx {
   int krylov_batch = 0;   // right-hand sides per Krylov sub-batch at most (0: as memory allows)
   bool factor_lookahead = true;
   // complex64 / split factorisation on the tensor cores (else the CUDA-core kernel)
-  bool factor_tc = true;
+  bool factor_tc = false;
+  // sweep-front shapes measured on the device on first use (else the cost model)
+  bool tune = true;
+  std::string dev_key;      // GPU identity for the tuner's cache (UUID, name, SM count)
+  double tune_seconds = 0;  // time this context spent measuring front shapes
   // bounded-wait limit of the sweep and factorisation kernels, in SM clock cycles
   long long wait_cycles = 4000000000LL;   // ~2 s at 2 GHz
   // device address of the allocation-free solve's fixed scratch array on this
@@ -177,7 +181,8 @@ size_t device_bytes(const lsw_ctx* c) {
              c->d_work.bytes + c->d_status.bytes + c->d_traces.bytes + c->d_outs.bytes + c->d_scratch.bytes +
              c->k_basis.bytes + c->k_zbasis.bytes + c->k_tmp.bytes + c->k_tmp2.bytes + c->k_r.bytes +
              c->k_part.bytes + c->k_small.bytes + c->k_small2.bytes + c->k_nrm.bytes + c->ls_items.bytes +
-             c->ls_slots.bytes + c->ls_scratch.bytes + c->h_b.bytes + c->h_x.bytes + c->d_ref.bytes;
+             c->ls_slots.bytes + c->ls_scratch.bytes + c->h_b.bytes + c->h_x.bytes + c->d_ref.bytes +
+             c->k_ls.bytes;
   for (auto& kv : c->sched_bufs)
     for (int i = 0; i < 3; ++i) b += kv.second[i].bytes;
   return b;
@@ -193,51 +198,226 @@ int fitting_cluster(const lsw_ctx* ctx, int slots, int cl) {
   return cl;   // nothing fits: the launch reports it
 }
 
-lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out) {
-  auto it = ctx->sched.find(nrhs);
+FrontPlan base_plan(const lsw_ctx* ctx) {
   const bool dbl = ctx->prec == LSW_PREC_C128;
+  FrontPlan plan;
+  plan.cluster_cap = std::max(1, std::min(4, ctx->max_cluster / 2));
+  plan.rmax = front_rmax(dbl);
+  plan.csize = dbl ? 16 : 8;
+  if (dbl) { plan.col_cost = 40.0; plan.col_slot_cost = 20.0; }
+  if (ctx->prec == LSW_PREC_SPLIT) {
+    // tensor-core matvec: the per-column cost hardly grows with the slots
+    plan.line_overhead = 2200.0; plan.slot_cost = 0.0; plan.col_cost = 40.0; plan.col_slot_cost = 3.0;
+  }
+  for (int cl = 1; cl <= 4; cl *= 2) plan.max_clusters[cl] = front_max_clusters(dbl, 2 * cl);
+  for (int r = 1; r <= 16; ++r)
+    plan.fit_mask[r] = front_fit_mask(dbl, ctx->prec == LSW_PREC_SPLIT, ctx->max_ny, ctx->max_nx, r);
+  if (plan.max_clusters[1] <= 0) plan.max_clusters[1] = ctx->nsm / 2;
+  return plan;
+}
+
+// A schedule's descriptors on the device (three buffers: items, slots, groups).
+lsw_status upload_schedule(lsw_ctx* ctx, Schedule* sc, const std::vector<DevItem>& items,
+                           const std::vector<DevSlot>& slots, const std::vector<DevGroup>& groups, DevBuf* bufs) {
+  CK(bufs[0].ensure(std::max<size_t>(1, items.size()) * sizeof(DevItem)), "cudaMalloc(items)");
+  CK(bufs[1].ensure(std::max<size_t>(1, slots.size()) * sizeof(DevSlot)), "cudaMalloc(slots)");
+  CK(bufs[2].ensure(std::max<size_t>(1, groups.size()) * sizeof(DevGroup)), "cudaMalloc(groups)");
+  CK(cudaMemcpy(bufs[0].p, items.data(), items.size() * sizeof(DevItem), cudaMemcpyHostToDevice), "H2D items");
+  CK(cudaMemcpy(bufs[1].p, slots.data(), slots.size() * sizeof(DevSlot), cudaMemcpyHostToDevice), "H2D slots");
+  CK(cudaMemcpy(bufs[2].p, groups.data(), groups.size() * sizeof(DevGroup), cudaMemcpyHostToDevice), "H2D groups");
+  sc->d_items = bufs[0].as<DevItem>();
+  sc->d_slots = bufs[1].as<DevSlot>();
+  sc->d_groups = bufs[2].as<DevGroup>();
+  sc->scratch_elems = 0;
+  for (auto& f : sc->fronts) sc->scratch_elems = std::max(sc->scratch_elems, f.scratch_elems);
+  return LSW_OK;
+}
+
+// the trace, output and scratch pools of a batch of nrhs right-hand sides
+lsw_status ensure_pools(lsw_ctx* ctx, int nrhs, long long scratch_elems) {
+  const size_t cs = csize(ctx->prec);
+  CK(ctx->d_traces.ensure((size_t)nrhs * 4 * ctx->ncell * 24 * ctx->LP * cs), "cudaMalloc(traces)");
+  CK(ctx->d_outs.ensure((size_t)nrhs * 4 * ctx->n2 * cs), "cudaMalloc(outs)");
+  CK(ctx->d_scratch.ensure(std::max<size_t>(1, (size_t)scratch_elems * cs)), "cudaMalloc(scratch)");
+  return LSW_OK;
+}
+
+lsw_status launch_front_of(lsw_ctx* ctx, const Schedule* sc, size_t fi, cudaStream_t st);
+lsw_status check_kernel_err(lsw_ctx* ctx, cudaStream_t st);
+
+// ---- sweep-front autotuner ----
+// On the first apply of a batch size the shape of every front -- slots per
+// item (4, 8, 16) and CTAs per half chain (1, 2, 4) -- is measured on the
+// device: each candidate shape is imposed on every front it fits, each front
+// whose launch is new is run twice and timed the second time with CUDA events
+// (the kernels' work does not depend on the values, so a zero vector serves),
+// and every front keeps its fastest shape.  The choices are kept per GPU and
+// problem shape (precision, cells, cell size, PML, batch size) for the
+// process, and in the file named by LSW_TUNE_CACHE when it is set.
+struct TuneEntry {
+  std::vector<int> r, cl;
+  std::vector<float> ms;
+};
+std::mutex g_tune_mu;
+std::map<std::string, TuneEntry> g_tune_cache;
+bool g_tune_file_read = false;
+
+std::string tune_key(const lsw_ctx* ctx, int nrhs) {
+  char b[160];
+  std::snprintf(b, sizeof(b), "|prec%d|N%d|m%d|p%d|rhs%d|cl%d", ctx->prec, ctx->N, ctx->m, ctx->p, nrhs,
+                ctx->max_cluster);
+  return ctx->dev_key + b;
+}
+
+void tune_file_read() {
+  if (g_tune_file_read) return;
+  g_tune_file_read = true;
+  const char* path = std::getenv("LSW_TUNE_CACHE");
+  if (!path || !*path) return;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return;
+  char line[65536];
+  while (std::fgets(line, sizeof(line), f)) {
+    char* save = nullptr;
+    char* tok = strtok_r(line, " \n", &save);
+    if (!tok) continue;
+    std::string key = tok;
+    TuneEntry e;
+    while ((tok = strtok_r(nullptr, " \n", &save))) {
+      int r = 0, cl = 0;
+      float ms = -1.f;
+      if (std::sscanf(tok, "%d,%d,%f", &r, &cl, &ms) != 3) { e.r.clear(); break; }
+      e.r.push_back(r); e.cl.push_back(cl); e.ms.push_back(ms);
+    }
+    if (!e.r.empty()) g_tune_cache[key] = e;
+  }
+  std::fclose(f);
+}
+
+void tune_file_append(const std::string& key, const TuneEntry& e) {
+  const char* path = std::getenv("LSW_TUNE_CACHE");
+  if (!path || !*path) return;
+  FILE* f = std::fopen(path, "a");
+  if (!f) return;
+  std::fprintf(f, "%s", key.c_str());
+  for (size_t i = 0; i < e.r.size(); ++i) std::fprintf(f, " %d,%d,%.5f", e.r[i], e.cl[i], e.ms[i]);
+  std::fprintf(f, "\n");
+  std::fclose(f);
+}
+
+lsw_status tune_fronts(lsw_ctx* ctx, int nrhs, const FrontPlan& plan, cudaStream_t st, TuneEntry* out) {
+  const auto t_start = std::chrono::steady_clock::now();
+  DevBuf tx, bufs[3];
+  CK(tx.ensure((size_t)nrhs * ctx->n2 * sizeof(double2)), "cudaMalloc(tuning vector)");
+  CK(cudaMemsetAsync(tx.p, 0, tx.bytes, st), "memset tuning vector");
+  CK(ctx->d_ref.ensure(2 * sizeof(void*)), "cudaMalloc(address table)");
+  KL(1, launch_set_refs(reinterpret_cast<const void**>(ctx->d_ref.p), tx.p, tx.p, st), "address table");
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CK(cudaEventCreate(&e0), "cudaEventCreate");
+  CK(cudaEventCreate(&e1), "cudaEventCreate");
+  std::vector<std::map<std::tuple<int, int, int>, float>> seen;   // per front: (items, max slots, cluster) -> ms
+  lsw_status s = LSW_OK;
+  for (int r : {4, 8, 16}) {
+    if (r > plan.rmax) continue;
+    for (int cl = 1; cl <= plan.cluster_cap && s == LSW_OK; cl *= 2) {
+      if (cl > 1 && plan.max_clusters[cl] <= 0) continue;
+      FrontPlan p = plan;
+      p.forced_r.assign(8 * (size_t)ctx->N + 8, r);
+      p.forced_cl.assign(8 * (size_t)ctx->N + 8, cl);
+      Schedule sc;
+      std::vector<DevItem> items; std::vector<DevSlot> slots; std::vector<DevGroup> groups;
+      try {
+        build_schedule(ctx->cells, ctx->N, nrhs, p, ctx->LP, sc.fronts, items, slots, groups, ctx->n2);
+      } catch (const std::exception&) {
+        continue;
+      }
+      if ((s = upload_schedule(ctx, &sc, items, slots, groups, bufs)) != LSW_OK) break;
+      if ((s = ensure_pools(ctx, nrhs, sc.scratch_elems)) != LSW_OK) break;
+      if (out->r.empty()) {
+        out->r.assign(sc.fronts.size(), 0);
+        out->cl.assign(sc.fronts.size(), 0);
+        out->ms.assign(sc.fronts.size(), 1e30f);
+        seen.assign(sc.fronts.size(), {});
+      }
+      for (size_t fi = 0; fi < sc.fronts.size() && s == LSW_OK; ++fi) {
+        const Front& f = sc.fronts[fi];
+        if (f.item_count <= 0 || f.slots_cap != r || f.cluster != cl) continue;   // shape did not fit here
+        const auto shape = std::make_tuple(f.item_count, f.max_slots, f.cluster);
+        float ms = 0.f;
+        auto hit = seen[fi].find(shape);
+        if (hit != seen[fi].end()) {
+          ms = hit->second;
+        } else {
+          if ((s = launch_front_of(ctx, &sc, fi, st)) != LSW_OK) break;
+          if (cudaEventRecord(e0, st) != cudaSuccess) { s = fail(ctx, LSW_ERR_CUDA, "event"); break; }
+          if ((s = launch_front_of(ctx, &sc, fi, st)) != LSW_OK) break;
+          if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+              cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+            s = fail(ctx, LSW_ERR_CUDA, "timing a sweep-front shape");
+            break;
+          }
+          seen[fi][shape] = ms;
+        }
+        if (ms < out->ms[fi] * 0.99f) { out->ms[fi] = ms; out->r[fi] = r; out->cl[fi] = cl; }
+      }
+      if (s == LSW_OK) s = check_kernel_err(ctx, st);
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CK(cudaStreamSynchronize(st), "tuning sync");
+  ctx->tune_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  return s;
+}
+
+lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out, cudaStream_t st) {
+  auto it = ctx->sched.find(nrhs);
+  void* const before[3] = {ctx->d_traces.p, ctx->d_outs.p, ctx->d_scratch.p};
   if (it == ctx->sched.end()) {
     std::unique_ptr<Schedule> sc(new Schedule);
     std::vector<DevItem> items; std::vector<DevSlot> slots; std::vector<DevGroup> groups;
+    FrontPlan plan;
     try {
-      FrontPlan plan;
-      plan.cluster_cap = std::max(1, std::min(4, ctx->max_cluster / 2));
-      plan.rmax = front_rmax(dbl);
-      plan.csize = dbl ? 16 : 8;
-      if (dbl) { plan.col_cost = 40.0; plan.col_slot_cost = 20.0; }
-      if (ctx->prec == LSW_PREC_SPLIT) {
-        // tensor-core matvec: the per-column cost hardly grows with the slots
-        plan.line_overhead = 2200.0; plan.slot_cost = 0.0; plan.col_cost = 40.0; plan.col_slot_cost = 3.0;
+      plan = base_plan(ctx);
+    } catch (const std::exception& ex) {
+      return fail(ctx, LSW_ERR_UNSUPPORTED, ex.what());
+    }
+    TuneEntry tuned;
+    if (ctx->tune && ctx->factorized) {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      tune_file_read();
+      const std::string key = tune_key(ctx, nrhs);
+      auto hit = g_tune_cache.find(key);
+      if (hit != g_tune_cache.end()) {
+        tuned = hit->second;
+      } else {
+        lsw_status s = tune_fronts(ctx, nrhs, plan, st, &tuned);
+        if (s != LSW_OK) return s;
+        g_tune_cache[key] = tuned;
+        tune_file_append(key, tuned);
       }
-      for (int cl = 1; cl <= 4; cl *= 2) plan.max_clusters[cl] = front_max_clusters(dbl, 2 * cl);
-      for (int r = 1; r <= 16; ++r)
-        plan.fit_mask[r] = front_fit_mask(dbl, ctx->prec == LSW_PREC_SPLIT, ctx->max_ny, ctx->max_nx, r);
-      if (plan.max_clusters[1] <= 0) plan.max_clusters[1] = ctx->nsm / 2;
+      plan.forced_r = tuned.r;
+      plan.forced_cl = tuned.cl;
+    }
+    try {
       build_schedule(ctx->cells, ctx->N, nrhs, plan, ctx->LP, sc->fronts, items, slots, groups, ctx->n2);
     } catch (const std::exception& ex) {
       return fail(ctx, LSW_ERR_UNSUPPORTED, ex.what());
     }
+    for (size_t fi = 0; fi < sc->fronts.size() && fi < tuned.r.size(); ++fi) {
+      Front& f = sc->fronts[fi];
+      if (f.slots_cap == tuned.r[fi] && f.cluster == tuned.cl[fi]) f.tuned_ms = tuned.ms[fi];
+    }
     sc->nrhs = nrhs;
-    for (auto& f : sc->fronts) sc->scratch_elems = std::max(sc->scratch_elems, f.scratch_elems);
     std::unique_ptr<DevBuf[]> bufs(new DevBuf[3]);
-    CK(bufs[0].ensure(std::max<size_t>(1, items.size()) * sizeof(DevItem)), "cudaMalloc(items)");
-    CK(bufs[1].ensure(std::max<size_t>(1, slots.size()) * sizeof(DevSlot)), "cudaMalloc(slots)");
-    CK(bufs[2].ensure(std::max<size_t>(1, groups.size()) * sizeof(DevGroup)), "cudaMalloc(groups)");
-    CK(cudaMemcpy(bufs[0].p, items.data(), items.size() * sizeof(DevItem), cudaMemcpyHostToDevice), "H2D items");
-    CK(cudaMemcpy(bufs[1].p, slots.data(), slots.size() * sizeof(DevSlot), cudaMemcpyHostToDevice), "H2D slots");
-    CK(cudaMemcpy(bufs[2].p, groups.data(), groups.size() * sizeof(DevGroup), cudaMemcpyHostToDevice), "H2D groups");
-    sc->d_items = bufs[0].as<DevItem>();
-    sc->d_slots = bufs[1].as<DevSlot>();
-    sc->d_groups = bufs[2].as<DevGroup>();
+    lsw_status s = upload_schedule(ctx, sc.get(), items, slots, groups, bufs.get());
+    if (s != LSW_OK) return s;
     ctx->sched_bufs[nrhs] = std::move(bufs);
     it = ctx->sched.emplace(nrhs, std::move(sc)).first;
   }
   Schedule* sc = it->second.get();
-  const size_t cs = csize(ctx->prec);
-  void* const before[3] = {ctx->d_traces.p, ctx->d_outs.p, ctx->d_scratch.p};
-  CK(ctx->d_traces.ensure((size_t)nrhs * 4 * ctx->ncell * 24 * ctx->LP * cs), "cudaMalloc(traces)");
-  CK(ctx->d_outs.ensure((size_t)nrhs * 4 * ctx->n2 * cs), "cudaMalloc(outs)");
-  CK(ctx->d_scratch.ensure(std::max<size_t>(1, (size_t)sc->scratch_elems * cs)), "cudaMalloc(scratch)");
+  lsw_status s = ensure_pools(ctx, nrhs, sc->scratch_elems);
+  if (s != LSW_OK) return s;
   if (before[0] != ctx->d_traces.p || before[1] != ctx->d_outs.p || before[2] != ctx->d_scratch.p) {
     // the captured applies point at the old pools
     for (auto& kv : ctx->graphs)
@@ -249,15 +429,9 @@ lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out) {
   return LSW_OK;
 }
 
-// The launches of one apply on stream st: clear the trace and output pools,
-// every sweep front, the sum of the four shifted outputs.  The input and
-// output addresses are read from ctx->d_ref (set by the caller beforehand),
-// so the sequence can be captured once and replayed for any vectors.
-// Returns the number of kernels enqueued in *kernels.
-lsw_status enqueue_apply(lsw_ctx* ctx, Schedule* sc, int nrhs, cudaStream_t st, int* kernels) {
-  const size_t cs = csize(ctx->prec);
-  CK(cudaMemsetAsync(ctx->d_traces.p, 0, (size_t)nrhs * 4 * ctx->ncell * 24 * ctx->LP * cs, st), "memset traces");
-  CK(cudaMemsetAsync(ctx->d_outs.p, 0, (size_t)nrhs * 4 * ctx->n2 * cs, st), "memset outs");
+// One sweep front of schedule sc on stream st.  The input and output
+// addresses are read from ctx->d_ref.
+lsw_status launch_front_of(lsw_ctx* ctx, const Schedule* sc, size_t fi, cudaStream_t st) {
   FrontArgs a{};
   a.cells = ctx->d_cells.as<DevCell>();
   a.slots = sc->d_slots;
@@ -274,19 +448,33 @@ lsw_status enqueue_apply(lsw_ctx* ctx, Schedule* sc, int nrhs, cudaStream_t st, 
   a.err = ctx->d_status.as<int>() + 1;
   a.wait_cycles = ctx->wait_cycles;
   a.split = ctx->prec == LSW_PREC_SPLIT ? 1 : 0;
+  const Front& f = sc->fronts[fi];
+  a.items = sc->d_items + f.item_begin;
+  a.item_count = f.item_count;
+  a.max_slots = f.max_slots;
+  a.cluster = f.cluster;
+  cudaError_t e = ctx->prec != LSW_PREC_C128 ? launch_front<float>(a, ctx->max_ny, ctx->max_nx, st)
+                                             : launch_front<double>(a, ctx->max_ny, ctx->max_nx, st);
+  CK(e, "front kernel");
+  return LSW_OK;
+}
+
+// The launches of one apply on stream st: clear the trace and output pools,
+// every sweep front, the sum of the four shifted outputs.  The input and
+// output addresses are read from ctx->d_ref (set by the caller beforehand),
+// so the sequence can be captured once and replayed for any vectors.
+// Returns the number of kernels enqueued in *kernels.
+lsw_status enqueue_apply(lsw_ctx* ctx, Schedule* sc, int nrhs, cudaStream_t st, int* kernels) {
+  const size_t cs = csize(ctx->prec);
+  CK(cudaMemsetAsync(ctx->d_traces.p, 0, (size_t)nrhs * 4 * ctx->ncell * 24 * ctx->LP * cs, st), "memset traces");
+  CK(cudaMemsetAsync(ctx->d_outs.p, 0, (size_t)nrhs * 4 * ctx->n2 * cs, st), "memset outs");
   int k = 0;
   for (size_t fi = 0; fi < sc->fronts.size(); ++fi) {
-    const Front& f = sc->fronts[fi];
-    a.items = sc->d_items + f.item_begin;
-    a.item_count = f.item_count;
-    a.max_slots = f.max_slots;
-    a.cluster = f.cluster;
     if (ctx->front_events) CK(cudaEventRecord((*ctx->front_events)[2 * fi], st), "event");
-    cudaError_t e = ctx->prec != LSW_PREC_C128 ? launch_front<float>(a, ctx->max_ny, ctx->max_nx, st)
-                                               : launch_front<double>(a, ctx->max_ny, ctx->max_nx, st);
-    CK(e, "front kernel");
+    lsw_status s = launch_front_of(ctx, sc, fi, st);
+    if (s != LSW_OK) return s;
     if (ctx->front_events) CK(cudaEventRecord((*ctx->front_events)[2 * fi + 1], st), "event");
-    k += f.item_count > 0 ? 1 : 0;
+    k += sc->fronts[fi].item_count > 0 ? 1 : 0;
   }
   double2* const* yref = reinterpret_cast<double2* const*>(ctx->d_ref.p) + 1;
   cudaError_t e = ctx->prec != LSW_PREC_C128 ? launch_combine_ref<float>(ctx->d_outs.p, yref, nrhs, ctx->n2, st)
@@ -298,7 +486,7 @@ lsw_status enqueue_apply(lsw_ctx* ctx, Schedule* sc, int nrhs, cudaStream_t st, 
 
 lsw_status precond_impl(lsw_ctx* ctx, const double2* x, double2* y, int nrhs, cudaStream_t st) {
   Schedule* sc = nullptr;
-  lsw_status s = ensure_batch(ctx, nrhs, &sc);
+  lsw_status s = ensure_batch(ctx, nrhs, &sc, st);
   if (s != LSW_OK) return s;
   CK(ctx->d_ref.ensure(2 * sizeof(void*)), "cudaMalloc(address table)");
   KL(1, launch_set_refs(reinterpret_cast<const void**>(ctx->d_ref.p), x, y, st), "address table");
@@ -472,8 +660,28 @@ lsw_status lsw_ctx_create(lsw_ctx** out, int device) {
   if (const char* ev = std::getenv("LSW_FACTOR_LOOKAHEAD")) c->factor_lookahead = std::atoi(ev) != 0;
   // LSW_GRAPHS=0 launches every apply's kernels one by one instead of replaying a CUDA graph
   if (const char* ev = std::getenv("LSW_GRAPHS")) c->use_graphs = std::atoi(ev) != 0;
-  // LSW_FACTOR_TC=0 runs the complex64 / split factorisation on the CUDA cores
+  // LSW_FACTOR_TC=1 runs the complex64 / split factorisation on the tensor cores
   if (const char* ev = std::getenv("LSW_FACTOR_TC")) c->factor_tc = std::atoi(ev) != 0;
+  // LSW_TUNE=0 leaves every sweep-front shape to the cost model
+  if (const char* ev = std::getenv("LSW_TUNE")) c->tune = std::atoi(ev) != 0;
+  {
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) {
+      char b[64];
+      std::string k;
+      for (int i = 0; i < 16; ++i) {
+        std::snprintf(b, sizeof(b), "%02x", (unsigned char)prop.uuid.bytes[i]);
+        k += b;
+      }
+      std::string name = prop.name;
+      for (char& ch : name)
+        if (ch == ' ' || ch == '|') ch = '_';
+      std::snprintf(b, sizeof(b), "|sm%d|", prop.multiProcessorCount);
+      c->dev_key = k + b + name;
+    } else {
+      c->dev_key = "unknown-gpu";
+    }
+  }
   // the host-side name of the allocation-free solve's scratch array is not a
   // device address: look the address up on this device (current since the
   // cudaSetDevice above) and keep it with the context
@@ -489,6 +697,43 @@ lsw_status lsw_ctx_create(lsw_ctx** out, int device) {
 lsw_status lsw_ctx_set_graphs(lsw_ctx* ctx, int enable) {
   if (!ctx) return LSW_ERR_INVALID_ARGUMENT;
   ctx->use_graphs = enable != 0;
+  return LSW_OK;
+}
+
+lsw_status lsw_ctx_set_tuning(lsw_ctx* ctx, int enable) {
+  if (!ctx) return LSW_ERR_INVALID_ARGUMENT;
+  if (ctx->tune != (enable != 0)) {
+    // the schedules built under the other setting are rebuilt on next use
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    CK(cudaDeviceSynchronize(), "sync");
+    ctx->drop_graphs();
+    ctx->sched.clear();
+    ctx->sched_bufs.clear();
+  }
+  ctx->tune = enable != 0;
+  return LSW_OK;
+}
+
+lsw_status lsw_front_shapes(lsw_ctx* ctx, int nrhs, lsw_front_shape* out, int capacity, int* n_fronts,
+                            double* tune_seconds, void* stream) {
+  if (!ctx || nrhs < 1 || !n_fronts || capacity < 0 || (capacity > 0 && !out))
+    return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "bad arguments to lsw_front_shapes");
+  if (!ctx->is_setup) return fail(ctx, LSW_ERR_NOT_SET_UP, "lsw_problem_setup first");
+  if (!ctx->factorized) return fail(ctx, LSW_ERR_NOT_FACTORIZED, "lsw_factorize first");
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  Schedule* sc = nullptr;
+  lsw_status s = ensure_batch(ctx, nrhs, &sc, S(stream));
+  if (s != LSW_OK) return s;
+  *n_fronts = (int)sc->fronts.size();
+  for (int i = 0; i < capacity && i < (int)sc->fronts.size(); ++i) {
+    const Front& f = sc->fronts[i];
+    out[i].items = f.item_count;
+    out[i].max_slots = f.max_slots;
+    out[i].slots_cap = f.slots_cap;
+    out[i].cluster = f.cluster;
+    out[i].tuned_ms = f.tuned_ms;
+  }
+  if (tune_seconds) *tune_seconds = ctx->tune_seconds;
   return LSW_OK;
 }
 
@@ -662,7 +907,7 @@ lsw_status lsw_apply_precond_profiled(lsw_ctx* ctx, const void* x, void* y, int 
   CK(cudaSetDevice(ctx->device), "cudaSetDevice");
   cudaStream_t st = S(stream);
   Schedule* sc = nullptr;
-  lsw_status s = ensure_batch(ctx, nrhs, &sc);
+  lsw_status s = ensure_batch(ctx, nrhs, &sc, st);
   if (s != LSW_OK) return s;
   std::vector<cudaEvent_t> ev(2 * sc->fronts.size() + 2);
   for (auto& e : ev) CK(cudaEventCreate(&e), "cudaEventCreate");
@@ -960,6 +1205,10 @@ static lsw_status gmres_reference(lsw_ctx* ctx, const double2* b, double2* x, in
   return LSW_OK;
 }
 
+// Right-preconditioned flexible GMRES(m) (Saad 1993) with modified Gram-Schmidt.
+// The Hessenberg least-squares problem (complex Givens rotations, the rotated
+// right-hand side, the back substitution at the end of a cycle) stays on the
+// device in FP64; an iteration reads back only the residual estimates.
 static lsw_status gmres_flexible(lsw_ctx* ctx, const double2* b, double2* x, int nv, const lsw_gmres_opts* o,
                                  lsw_gmres_report* rep, cudaStream_t st) {
   const long long n2 = ctx->n2;
@@ -970,14 +1219,27 @@ static lsw_status gmres_flexible(lsw_ctx* ctx, const double2* b, double2* x, int
   CK(ctx->k_tmp.ensure(vb), "cudaMalloc(tmp)");
   CK(ctx->k_part.ensure((size_t)nv * 1216 * sizeof(double2)), "cudaMalloc(partials)");
   CK(ctx->k_small.ensure((size_t)nv * (m + 2) * sizeof(double2) + 64), "cudaMalloc(h)");
-  CK(ctx->k_small2.ensure((size_t)nv * (m + 2) * sizeof(double2) + 64), "cudaMalloc(coef)");
   CK(ctx->k_nrm.ensure((size_t)nv * 2 * sizeof(double2) + 64), "cudaMalloc(nrm)");
+  // least-squares state: H, cs, sn, coef, g, sc (complex); ||b||, est (2 nv), rel (real); active (int)
+  const size_t nH = (size_t)nv * (m + 1) * m, nR = (size_t)nv * m, nG = (size_t)nv * (m + 1);
+  const size_t cplx_n = nH + 3 * nR + nG + (size_t)nv;
+  CK(ctx->k_ls.ensure(cplx_n * sizeof(double2) + 4 * (size_t)nv * sizeof(double) + (size_t)nv * sizeof(int) + 64),
+     "cudaMalloc(least squares)");
+  double2* Hd = ctx->k_ls.as<double2>();
+  double2* csd = Hd + nH;
+  double2* snd = csd + nR;
+  double2* coefd = snd + nR;
+  double2* gd = coefd + nR;
+  double2* scd = gd + nG;
+  double* bnd = reinterpret_cast<double*>(scd + nv);
+  double* estd = bnd + nv;
+  double* reld = estd + 2 * nv;
+  int* actd = reinterpret_cast<int*>(reld + nv);
   double2* V = ctx->k_basis.as<double2>();
   double2* Z = ctx->k_zbasis.as<double2>();
   double2* tmp = ctx->k_tmp.as<double2>();
   double2* part = ctx->k_part.as<double2>();
   double2* hdev = ctx->k_small.as<double2>();
-  double2* cdev = ctx->k_small2.as<double2>();
   double* ndev = ctx->k_nrm.as<double>();
   auto Vi = [&](int i) { return V + (size_t)i * nv * n2; };
   auto Zi = [&](int i) { return Z + (size_t)i * nv * n2; };
@@ -989,32 +1251,26 @@ static lsw_status gmres_flexible(lsw_ctx* ctx, const double2* b, double2* x, int
   CK(cudaMemcpyAsync(bn.data(), ndev, nv * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
   CK(cudaStreamSynchronize(st), "sync");
   for (auto& q : bn) q = std::sqrt(q);
-  std::vector<double> rel(nv, 1.0), log0;
-  std::vector<int> conv(nv, 0);
+  CK(cudaMemcpyAsync(bnd, bn.data(), nv * sizeof(double), cudaMemcpyHostToDevice, st), "H2D |b|");
+  std::vector<double> rel(nv, 1.0), est(2 * (size_t)nv, 0.0), log0;
+  std::vector<int> active(nv, 1);
   while (true) {
-    // r = b - A x
+    // r = b - A x, its norm, the cycle's least-squares state
     if ((s = apply_A_impl(ctx, x, tmp, nv, st)) != LSW_OK) return s;
     for (int v = 0; v < nv; ++v) KL(1, launch_sub(Vi(0) + v * n2, b + v * n2, tmp + v * n2, n2, st), "sub");
     KL(2, launch_norm2(Vi(0), n2, nv, n2, reinterpret_cast<double*>(part), ndev, st), "norm r");
-    std::vector<double> rn(nv);
-    CK(cudaMemcpyAsync(rn.data(), ndev, nv * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+    KL(1, launch_fgmres_init(nv, m, ndev, bnd, o->tol, scd, gd, reld, actd, st), "least squares init");
+    CK(cudaMemcpyAsync(rel.data(), reld, nv * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
     CK(cudaStreamSynchronize(st), "sync");
-    std::vector<double2> sc(nv);
+    bool all_conv = true;
     for (int v = 0; v < nv; ++v) {
-      rn[v] = std::sqrt(rn[v]);
-      rel[v] = bn[v] > 0 ? rn[v] / bn[v] : 0.0;
-      conv[v] = rel[v] <= o->tol ? 1 : 0;
-      sc[v] = make_double2(rn[v] > 0 ? rn[v] : 1.0, 0.0);
+      active[v] = rel[v] <= o->tol ? 0 : 1;
+      all_conv = all_conv && !active[v];
     }
     log0.push_back(rel[0]);
     if (o->verbose) printf("fgmres it %d: true rel. residual %.6e\n", it, rel[0]);
-    if (std::all_of(conv.begin(), conv.end(), [](int c) { return c != 0; }) || it >= o->max_iter) break;
-    CK(cudaMemcpyAsync(cdev, sc.data(), nv * sizeof(double2), cudaMemcpyHostToDevice, st), "H2D");
-    KL(1, launch_scale(Vi(0), Vi(0), cdev, 1, n2, nv, n2, st), "scale");
-    std::vector<std::vector<cplx>> H(nv, std::vector<cplx>((size_t)(m + 1) * m)), g(nv, std::vector<cplx>(m + 1));
-    std::vector<std::vector<cplx>> cs(nv, std::vector<cplx>(m)), sn(nv, std::vector<cplx>(m));
-    std::vector<int> active(nv);
-    for (int v = 0; v < nv; ++v) { g[v][0] = rn[v]; active[v] = conv[v] ? 0 : 1; }
+    if (all_conv || it >= o->max_iter) break;
+    KL(1, launch_scale(Vi(0), Vi(0), scd, 1, n2, nv, n2, st), "scale");
     int ncol = 0;
     for (int j = 0; j < m; ++j) {
       if ((s = precond_impl(ctx, Vi(j), Zi(j), nv, st)) != LSW_OK) return s;
@@ -1031,59 +1287,27 @@ static lsw_status gmres_flexible(lsw_ctx* ctx, const double2* b, double2* x, int
           KL(2, launch_axpy_dot(w, Vi(i), hdev + (size_t)i * nv, nullptr, n2, nv, n2, part,
                              hdev + (size_t)(j + 1) * nv, 0, st), "axpy_norm");
       }
-      std::vector<double2> hh((size_t)(j + 2) * nv);
-      CK(cudaMemcpyAsync(hh.data(), hdev, hh.size() * sizeof(double2), cudaMemcpyDeviceToHost, st), "D2H h");
+      KL(1, launch_fgmres_givens(j, nv, m, hdev, Hd, csd, snd, gd, scd, estd, bnd, st), "givens");
+      KL(1, launch_scale(w, w, scd, 1, n2, nv, n2, st), "scale");
+      CK(cudaMemcpyAsync(est.data(), estd, 2 * nv * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H estimate");
       CK(cudaStreamSynchronize(st), "sync");
       ++it;
       ncol = j + 1;
       bool all_small = true;
-      for (int v = 0; v < nv; ++v) {
-        std::vector<cplx> h(j + 2);
-        for (int i = 0; i <= j; ++i) h[i] = cplx(hh[(size_t)i * nv + v].x, hh[(size_t)i * nv + v].y);
-        const double hn_ = std::sqrt(hh[(size_t)(j + 1) * nv + v].x);
-        h[j + 1] = hn_;
-        sc[v] = make_double2(hn_ > 0 ? hn_ : 1.0, 0.0);
-        for (int i = 0; i < j; ++i) {
-          const cplx t = std::conj(cs[v][i]) * h[i] + std::conj(sn[v][i]) * h[i + 1];
-          h[i + 1] = -sn[v][i] * h[i] + cs[v][i] * h[i + 1];
-          h[i] = t;
-        }
-        const double den = std::sqrt(std::norm(h[j]) + std::norm(h[j + 1]));
-        cs[v][j] = den > 0 ? h[j] / den : cplx(1, 0);
-        sn[v][j] = den > 0 ? h[j + 1] / den : cplx(0, 0);
-        h[j] = den;
-        h[j + 1] = 0.0;
-        g[v][j + 1] = -sn[v][j] * g[v][j];
-        g[v][j] = std::conj(cs[v][j]) * g[v][j];
-        for (int i = 0; i <= j + 1; ++i) H[v][(size_t)i * m + j] = h[i];
-        const double est = bn[v] > 0 ? std::abs(g[v][j + 1]) / bn[v] : 0.0;
-        if (v == 0) log0.push_back(est);
-        if (active[v] && est > o->tol && hn_ > 0) all_small = false;
-      }
+      for (int v = 0; v < nv; ++v)
+        if (active[v] && est[v] > o->tol && est[nv + v] > 0) all_small = false;
+      log0.push_back(est[0]);
       if (o->verbose) printf("fgmres it %d: estimate %.6e\n", it, log0.back());
-      CK(cudaMemcpyAsync(cdev, sc.data(), nv * sizeof(double2), cudaMemcpyHostToDevice, st), "H2D");
-      KL(1, launch_scale(w, w, cdev, 1, n2, nv, n2, st), "scale");
       if (all_small || it >= o->max_iter) break;
     }
-    // x += Z y  with y from the triangular system R y = g
-    std::vector<double2> coef((size_t)nv * ncol, make_double2(0, 0));
-    for (int v = 0; v < nv; ++v) {
-      if (!active[v]) continue;
-      std::vector<cplx> y(ncol);
-      for (int i = ncol - 1; i >= 0; --i) {
-        cplx sm = g[v][i];
-        for (int q = i + 1; q < ncol; ++q) sm -= H[v][(size_t)i * m + q] * y[q];
-        y[i] = H[v][(size_t)i * m + i] != cplx(0, 0) ? sm / H[v][(size_t)i * m + i] : cplx(0, 0);
-      }
-      for (int i = 0; i < ncol; ++i) coef[(size_t)v * ncol + i] = make_double2(y[i].real(), y[i].imag());
-    }
-    CK(ctx->k_small2.ensure(coef.size() * sizeof(double2) + 64), "cudaMalloc(coef)");
-    cdev = ctx->k_small2.as<double2>();
-    CK(cudaMemcpyAsync(cdev, coef.data(), coef.size() * sizeof(double2), cudaMemcpyHostToDevice, st), "H2D y");
-    KL(1, launch_lincomb(x, Z, (long long)nv * n2, n2, cdev, ncol, n2, nv, n2, st), "lincomb");
+    // x += Z y with y from the triangular system R y = g
+    KL(1, launch_fgmres_solve(ncol, nv, m, Hd, gd, actd, coefd, st), "least squares solve");
+    KL(1, launch_lincomb(x, Z, (long long)nv * n2, n2, coefd, ncol, n2, nv, n2, st), "lincomb");
   }
+  // the largest relative residual; a NaN (a non-finite solve) propagates
   double worst = 0.0;
-  for (int v = 0; v < nv; ++v) worst = std::max(worst, rel[v]);
+  for (int v = 0; v < nv; ++v)
+    if (!(rel[v] <= worst)) worst = rel[v];
   if (rep) {
     rep->iterations = it;
     rep->final_log = worst;
@@ -1113,8 +1337,12 @@ static lsw_status true_residual(lsw_ctx* ctx, const double2* b, const double2* x
   std::vector<double> h(2 * nv);
   CK(cudaMemcpyAsync(h.data(), nd, 2 * nv * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
   CK(cudaStreamSynchronize(st), "sync");
+  // the largest relative residual; a NaN (a non-finite solution) propagates
   *worst = 0.0;
-  for (int v = 0; v < nv; ++v) *worst = std::max(*worst, h[nv + v] > 0 ? std::sqrt(h[v] / h[nv + v]) : 0.0);
+  for (int v = 0; v < nv; ++v) {
+    const double rv = h[nv + v] > 0 ? std::sqrt(h[v] / h[nv + v]) : 0.0;
+    if (!(rv <= *worst)) *worst = rv;
+  }
   return LSW_OK;
 }
 
@@ -1160,9 +1388,9 @@ lsw_status lsw_gmres(lsw_ctx* ctx, const void* b, void* x, int nrhs, const lsw_g
     if (s != LSW_OK) return s;
     double t = 0.0;
     if ((s = true_residual(ctx, bb + (size_t)c0 * n2, xx + (size_t)c0 * n2, nv, &t, st)) != LSW_OK) return s;
-    tr = std::max(tr, t);
+    if (!(t <= tr)) tr = t;   // NaN propagates
     acc.iterations = std::max(acc.iterations, sub.iterations);
-    acc.final_log = std::max(acc.final_log, sub.final_log);
+    if (!(sub.final_log <= acc.final_log)) acc.final_log = sub.final_log;
     acc.precond_applies += sub.precond_applies;
     acc.converged = acc.converged && sub.converged;
     if (c0 == 0) acc.log_len = sub.log_len;
@@ -1210,7 +1438,7 @@ lsw_status lsw_release_workspace(lsw_ctx* ctx) {
   ctx->sched.clear();
   ctx->sched_bufs.clear();
   for (DevBuf* b : {&ctx->d_traces, &ctx->d_outs, &ctx->d_scratch, &ctx->k_basis, &ctx->k_zbasis, &ctx->k_tmp,
-                    &ctx->k_tmp2, &ctx->k_r, &ctx->k_part, &ctx->k_small, &ctx->k_small2, &ctx->k_nrm,
+                    &ctx->k_tmp2, &ctx->k_r, &ctx->k_part, &ctx->k_small, &ctx->k_small2, &ctx->k_nrm, &ctx->k_ls,
                     &ctx->ls_items, &ctx->ls_slots, &ctx->ls_scratch, &ctx->h_b, &ctx->h_x})
     b->release();
   return LSW_OK;

@@ -294,7 +294,8 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
     }
   };
   fronts.clear(); items.clear(); slots.clear(); groups.clear();
-  for (auto& f : fr) {
+  for (size_t fidx = 0; fidx < fr.size(); ++fidx) {
+    auto& f = fr[fidx];
     for (auto& kv : f)
       std::stable_sort(kv.second.begin(), kv.second.end(), [](const SlotSpec& a, const SlotSpec& b) {
         return std::make_tuple(a.rhs, a.shift, a.order) < std::make_tuple(b.rhs, b.shift, b.order);
@@ -309,41 +310,52 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
     int best_r = plan.rmax, best_cl = 1;
     double best_t = 1e300;
     long long best_items = 0;
-    for (int r : {16, 8, 4}) {
-      if (r > plan.rmax) continue;
-      long long n_items = 0;
-      int maxs = 0;
-      fac_elems = 0.0;
-      for (auto& kv : f) {
-        const DevCell& cl = cells[kv.first];
-        flatten(kv.second, r, [&](const std::vector<std::pair<size_t, size_t>>&, int count) {
-          ++n_items;
-          maxs = std::max(maxs, count);
-          fac_elems += 2.0 * cl.nx * (double)cl.ny * cl.ldn;
-        });
-      }
-      if (n_items == 0) continue;
-      const int R = front_rpad(maxs);
-      // an item is a cluster of two halves of cl CTAs, each running
-      // 2 nf + 1 lines of the twisted solve (nf forward lines of the longer half)
-      const int nf = nx_max - 1 - (nx_max - 1) / 2;
-      for (int cl = 1; cl <= plan.cluster_cap; cl *= 2) {
-        const int mc = std::max(1, plan.max_clusters[cl]);
-        if (plan.max_clusters[cl] <= 0 && cl > 1) continue;
-        if (!(plan.fit_mask[R] & (1 << cl))) continue;   // shared memory
-        const long long waves = (n_items + mc - 1) / mc;
-        const double line = plan.line_overhead + plan.slot_cost * R +
-                            (plan.col_cost + plan.col_slot_cost * R) * ((ny_max + cl - 1) / cl);
-        double t = (double)waves * (2.0 * nf + 1.0) * line;
-        t = std::max(t, fac_elems * plan.csize / plan.bytes_per_cycle);
-        // ties go to fewer items (less factor traffic), then to larger clusters
-        if (t < best_t * 0.98 || (t <= best_t * 1.02 && n_items < best_items)) {
-          best_t = t; best_r = r; best_cl = cl; best_items = n_items;
+    // fr_r / fr_cl > 0 restrict the search to that shape
+    auto search = [&](int fr_r, int fr_cl) {
+      for (int r : {16, 8, 4}) {
+        if (r > plan.rmax) continue;
+        if (fr_r > 0 && r != fr_r) continue;
+        long long n_items = 0;
+        int maxs = 0;
+        fac_elems = 0.0;
+        for (auto& kv : f) {
+          const DevCell& cl = cells[kv.first];
+          flatten(kv.second, r, [&](const std::vector<std::pair<size_t, size_t>>&, int count) {
+            ++n_items;
+            maxs = std::max(maxs, count);
+            fac_elems += 2.0 * cl.nx * (double)cl.ny * cl.ldn;
+          });
+        }
+        if (n_items == 0) continue;
+        const int R = front_rpad(maxs);
+        // an item is a cluster of two halves of cl CTAs, each running
+        // 2 nf + 1 lines of the twisted solve (nf forward lines of the longer half)
+        const int nf = nx_max - 1 - (nx_max - 1) / 2;
+        for (int cl = 1; cl <= plan.cluster_cap; cl *= 2) {
+          if (fr_cl > 0 && cl != fr_cl) continue;
+          const int mc = std::max(1, plan.max_clusters[cl]);
+          if (plan.max_clusters[cl] <= 0 && cl > 1) continue;
+          if (!(plan.fit_mask[R] & (1 << cl))) continue;   // shared memory
+          const long long waves = (n_items + mc - 1) / mc;
+          const double line = plan.line_overhead + plan.slot_cost * R +
+                              (plan.col_cost + plan.col_slot_cost * R) * ((ny_max + cl - 1) / cl);
+          double t = (double)waves * (2.0 * nf + 1.0) * line;
+          t = std::max(t, fac_elems * plan.csize / plan.bytes_per_cycle);
+          // ties go to fewer items (less factor traffic), then to larger clusters
+          if (t < best_t * 0.98 || (t <= best_t * 1.02 && n_items < best_items)) {
+            best_t = t; best_r = r; best_cl = cl; best_items = n_items;
+          }
         }
       }
-    }
+    };
+    const int fr_r = fidx < plan.forced_r.size() ? plan.forced_r[fidx] : 0;
+    const int fr_cl = fidx < plan.forced_cl.size() ? plan.forced_cl[fidx] : 0;
+    search(fr_r, fr_cl);
+    // a fixed shape that does not fit this front leaves it to the cost model
+    if (best_t >= 1e300 && (fr_r > 0 || fr_cl > 0)) search(0, 0);
     if (best_t >= 1e300) throw std::runtime_error("no sweep-front launch shape fits in shared memory");
     Front F{(int)items.size(), 0, 0, 0, best_cl};
+    F.slots_cap = best_r;
     for (auto& kv : f) {
       const int c = kv.first;
       auto& v = kv.second;

@@ -94,6 +94,8 @@ struct Front {
   long long scratch_elems;
   int max_slots;
   int cluster;            // CTAs per item chosen for this front
+  int slots_cap = 0;      // slots per item at most (the planner's r)
+  float tuned_ms = -1.f;  // the tuner's timing of this shape, -1 when the cost model chose it
 };
 
 // What the front planner knows about the device: how many clusters of each
@@ -114,6 +116,10 @@ struct FrontPlan {
   double col_cost = 25.0;
   double col_slot_cost = 10.0;
   double bytes_per_cycle = 3300.0;
+  // shapes fixed per front (slots per item, CTAs per half), e.g. by the
+  // autotuner; an entry of 0, a missing entry or a shape that does not fit
+  // leaves the front to the cost model
+  std::vector<int> forced_r, forced_cl;
 };
 
 struct Schedule {
@@ -231,5 +237,12 @@ cudaError_t launch_lincomb(double2* y, const double2* basis, long long basis_str
                            long long basis_stride_rhs, const double2* coef, int ncoef, long long n,
                            int nvec, long long y_stride, cudaStream_t st); // y[v] += sum_i coef[v][i] basis[i][v]
 cudaError_t launch_sub(double2* y, const double2* a, const double2* b, long long n, cudaStream_t st);
+// FGMRES(m) Hessenberg least squares on the device, one thread per right-hand side
+cudaError_t launch_fgmres_init(int nv, int m, const double* r2, const double* bn, double tol, double2* sc, double2* g,
+                               double* rel, int* active, cudaStream_t st);
+cudaError_t launch_fgmres_givens(int j, int nv, int m, const double2* h, double2* H, double2* cs, double2* sn,
+                                 double2* g, double2* sc, double* est, const double* bn, cudaStream_t st);
+cudaError_t launch_fgmres_solve(int ncol, int nv, int m, const double2* H, const double2* g, const int* active,
+                                double2* coef, cudaStream_t st);
 
 }  // namespace lsw

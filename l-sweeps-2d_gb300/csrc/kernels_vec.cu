@@ -303,4 +303,107 @@ cudaError_t launch_sub(double2* y, const double2* a, const double2* b, long long
   return cudaGetLastError();
 }
 
+// ---- the Hessenberg least-squares problem of FGMRES(m) on the device ----
+// One thread per right-hand side v.  H is (m + 1) x m row-major, cs and sn the
+// m Givens rotations, g the rotated right-hand side (m + 1), all FP64 complex.
+namespace {
+__device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+
+// start of a cycle: ||r|| from its square, the relative residual, whether the
+// right-hand side still iterates, ||r|| as V_0's divisor (1 if zero), and
+// g = (||r||, 0, ..., 0)
+__global__ void k_fgmres_init(int nv, int m, const double* __restrict__ r2, const double* __restrict__ bn,
+                              double tol, double2* __restrict__ sc, double2* __restrict__ g, double* __restrict__ rel,
+                              int* __restrict__ active) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const double rn = sqrt(r2[v]);
+  const double rv = bn[v] > 0 ? rn / bn[v] : 0.0;
+  rel[v] = rv;
+  active[v] = rv <= tol ? 0 : 1;
+  sc[v] = make_double2(rn > 0 ? rn : 1.0, 0.0);
+  double2* gv = g + (size_t)v * (m + 1);
+  gv[0] = make_double2(rn, 0.0);
+  for (int i = 1; i <= m; ++i) gv[i] = make_double2(0.0, 0.0);
+}
+
+// step j: column j of H from the Gram-Schmidt coefficients h_0..h_j and
+// ||w||^2 (row j + 1, real part); rotations 0..j-1 applied to it, rotation j
+// formed (cs = h_j / d, sn = h_{j+1} / d, d = (|h_j|^2 + |h_{j+1}|^2)^(1/2)),
+// g rotated; sc = ||w|| (the next basis vector's divisor, 1 if zero),
+// est[v] = |g_{j+1}| / ||b||, est[nv + v] = ||w|| (0 on a breakdown)
+__global__ void k_fgmres_givens(int j, int nv, int m, const double2* __restrict__ h, double2* __restrict__ H,
+                                double2* __restrict__ cs, double2* __restrict__ sn, double2* __restrict__ g,
+                                double2* __restrict__ sc, double* __restrict__ est, const double* __restrict__ bn) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  double2* Hv = H + (size_t)v * (m + 1) * m;
+  double2* csv = cs + (size_t)v * m;
+  double2* snv = sn + (size_t)v * m;
+  double2* gv = g + (size_t)v * (m + 1);
+  const double hn = sqrt(h[(size_t)(j + 1) * nv + v].x);
+  double2 col[2];
+  double2 prev = h[v];
+  for (int i = 0; i < j; ++i) {
+    const double2 b = h[(size_t)(i + 1) * nv + v];
+    col[0] = cadd(cmul(cconj(csv[i]), prev), cmul(cconj(snv[i]), b));
+    col[1] = csub(cmul(csv[i], b), cmul(snv[i], prev));
+    Hv[(size_t)i * m + j] = col[0];
+    prev = col[1];
+  }
+  // prev: rotated h_j; the subdiagonal entry is ||w||
+  const double2 a = prev, b = make_double2(hn, 0.0);
+  const double den = sqrt(abs2(a) + abs2(b));
+  const double2 c = den > 0 ? make_double2(a.x / den, a.y / den) : make_double2(1.0, 0.0);
+  const double2 s = den > 0 ? make_double2(b.x / den, b.y / den) : make_double2(0.0, 0.0);
+  csv[j] = c;
+  snv[j] = s;
+  Hv[(size_t)j * m + j] = make_double2(den, 0.0);
+  Hv[(size_t)(j + 1) * m + j] = make_double2(0.0, 0.0);
+  const double2 gj = gv[j];
+  gv[j + 1] = cneg(cmul(s, gj));
+  gv[j] = cmul(cconj(c), gj);
+  sc[v] = make_double2(hn > 0 ? hn : 1.0, 0.0);
+  est[v] = bn[v] > 0 ? sqrt(abs2(gv[j + 1])) / bn[v] : 0.0;
+  est[nv + v] = hn;
+}
+
+// end of a cycle: y = R^-1 g by back substitution on the first ncol columns
+// (zero for right-hand sides that did not iterate), into coef[v][0..ncol)
+__global__ void k_fgmres_solve(int ncol, int nv, int m, const double2* __restrict__ H, const double2* __restrict__ g,
+                               const int* __restrict__ active, double2* __restrict__ coef) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const double2* Hv = H + (size_t)v * (m + 1) * m;
+  const double2* gv = g + (size_t)v * (m + 1);
+  double2* y = coef + (size_t)v * ncol;
+  for (int i = ncol - 1; i >= 0; --i) {
+    if (!active[v]) {
+      y[i] = make_double2(0.0, 0.0);
+      continue;
+    }
+    double2 sm = gv[i];
+    for (int q = i + 1; q < ncol; ++q) cfms(sm, Hv[(size_t)i * m + q], y[q]);
+    const double2 d = Hv[(size_t)i * m + i];
+    y[i] = (d.x != 0.0 || d.y != 0.0) ? cmul(sm, crcp(d)) : make_double2(0.0, 0.0);
+  }
+}
+}  // namespace
+
+cudaError_t launch_fgmres_init(int nv, int m, const double* r2, const double* bn, double tol, double2* sc, double2* g,
+                               double* rel, int* active, cudaStream_t st) {
+  k_fgmres_init<<<(nv + 63) / 64, 64, 0, st>>>(nv, m, r2, bn, tol, sc, g, rel, active);
+  return cudaGetLastError();
+}
+cudaError_t launch_fgmres_givens(int j, int nv, int m, const double2* h, double2* H, double2* cs, double2* sn,
+                                 double2* g, double2* sc, double* est, const double* bn, cudaStream_t st) {
+  k_fgmres_givens<<<(nv + 63) / 64, 64, 0, st>>>(j, nv, m, h, H, cs, sn, g, sc, est, bn);
+  return cudaGetLastError();
+}
+cudaError_t launch_fgmres_solve(int ncol, int nv, int m, const double2* H, const double2* g, const int* active,
+                                double2* coef, cudaStream_t st) {
+  k_fgmres_solve<<<(nv + 63) / 64, 64, 0, st>>>(ncol, nv, m, H, g, active, coef);
+  return cudaGetLastError();
+}
+
 }  // namespace lsw

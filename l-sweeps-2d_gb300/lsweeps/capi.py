@@ -22,7 +22,8 @@ EXPORTS = [
     "lsw_problem_setup", "lsw_problem_info_get", "lsw_cell_info_get", "lsw_factorize", "lsw_apply_precond",
     "lsw_apply_A", "lsw_assemble_rhs", "lsw_gmres", "lsw_solve_host", "lsw_local_solve",
     "lsw_apply_precond_profiled", "lsw_local_solve_noalloc", "lsw_release_workspace",
-    "lsw_ctx_set_wait_limit", "lsw_selftest_bounded_wait", "lsw_ctx_set_graphs",
+    "lsw_ctx_set_wait_limit", "lsw_selftest_bounded_wait", "lsw_ctx_set_graphs", "lsw_ctx_set_tuning",
+    "lsw_front_shapes",
 ]
 
 
@@ -53,6 +54,11 @@ class CellInfo(C.Structure):
         return dict(I=self.I, J=self.J, nx=self.nx, ny=self.ny, lo_x=self.lo_x, lo_y=self.lo_y,
                     lines_x=[list(r) for r in self.lines_x], lines_y=[list(r) for r in self.lines_y],
                     own_x=[list(r) for r in self.own_x], own_y=[list(r) for r in self.own_y])
+
+
+class FrontShape(C.Structure):
+    _fields_ = [("items", C.c_int), ("max_slots", C.c_int), ("slots_cap", C.c_int), ("cluster", C.c_int),
+                ("tuned_ms", C.c_float)]
 
 
 class GmresOpts(C.Structure):
@@ -107,6 +113,8 @@ def lib() -> C.CDLL:
         "lsw_ctx_set_wait_limit": (i, [vp, d]),
         "lsw_selftest_bounded_wait": (i, [vp, vp]),
         "lsw_ctx_set_graphs": (i, [vp, i]),
+        "lsw_ctx_set_tuning": (i, [vp, i]),
+        "lsw_front_shapes": (i, [vp, i, C.POINTER(FrontShape), i, C.POINTER(i), C.POINTER(d), vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -99,6 +99,25 @@ class Solver:
     def factorize(self, stream=None):
         capi.check(self.L.lsw_factorize(self.ctx, _stream_ptr(stream)), self.ctx)
 
+    def front_shapes(self, nrhs: int = 1, stream=None) -> tuple[list[dict], float]:
+        """The sweep fronts' launch shapes for a batch of nrhs right-hand sides
+        (lsw_front_shapes) and the context's tuning time in seconds."""
+        n = C.c_int(0)
+        ts = C.c_double(0.0)
+        cap = 4 * self.spec.N + 8
+        buf = (capi.FrontShape * cap)()
+        capi.check(self.L.lsw_front_shapes(self.ctx, nrhs, buf, cap, C.byref(n), C.byref(ts), _stream_ptr(stream)),
+                   self.ctx)
+        return [{k: getattr(buf[i], k) for k, _ in capi.FrontShape._fields_} for i in range(n.value)], ts.value
+
+    def set_tuning(self, enable: bool):
+        """Measure sweep-front shapes on first use (lsw_ctx_set_tuning)."""
+        capi.check(self.L.lsw_ctx_set_tuning(self.ctx, 1 if enable else 0), self.ctx)
+
+    def set_graphs(self, enable: bool):
+        """Replay applies as CUDA graphs (lsw_ctx_set_graphs)."""
+        capi.check(self.L.lsw_ctx_set_graphs(self.ctx, 1 if enable else 0), self.ctx)
+
     def release_workspace(self):
         """Free the Krylov bases and sweep pools (lsw_release_workspace); the factors stay."""
         capi.check(self.L.lsw_release_workspace(self.ctx), self.ctx)
