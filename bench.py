@@ -292,6 +292,9 @@ def run_gpu(args):
         b = S.assemble_rhs(spec.sources)
     nrhs = b.numel() // S.n2
     x = torch.empty_like(b)
+    # the sweep-front launch shapes of this batch size are measured (or read
+    # from the tuner's cache) before anything is timed
+    S.front_shapes(nrhs)
 
     def solve():
         return S.gmres(b, mode="flexible", tol=args.tol, max_iter=300, restart=30, x=x)
@@ -397,6 +400,7 @@ def run_gpu(args):
         e1.record(st)
         torch.cuda.synchronize()
         f64_fact = e0.elapsed_time(e1) / 1e3
+        S64.front_shapes(nrhs)
         x64 = torch.empty_like(b)
         if args.fp64_warmup:
             S64.gmres(b, mode="flexible", tol=args.tol, max_iter=300, restart=30, x=x64)

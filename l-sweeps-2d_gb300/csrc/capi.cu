@@ -77,6 +77,7 @@ struct lsw_ctx {
   bool tune = true;
   std::string dev_key;      // GPU identity for the tuner's cache (UUID, name, SM count)
   double tune_seconds = 0;  // time this context spent measuring front shapes
+  int force_r = 0, force_cl = 0;   // one launch shape imposed on every front where it fits
   // bounded-wait limit of the sweep and factorisation kernels, in SM clock cycles
   long long wait_cycles = 4000000000LL;   // ~2 s at 2 GHz
   // device address of the allocation-free solve's fixed scratch array on this
@@ -139,16 +140,17 @@ lsw_status cuda_fail(lsw_ctx* c, cudaError_t e, const char* where) {
 inline size_t csize(int prec) { return prec == LSW_PREC_C128 ? 16 : 8; }
 inline cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
-DevCell make_cell(int I, int J, int N, int m, int p, bool split) {
+DevCell make_cell(int I, int J, int N, int m, int p, bool fp32_factors) {
   DevCell c{};
   const DirGeom gx = dir_geom(J, N, m, p), gy = dir_geom(I, N, m, p);
   c.I = I; c.J = J;
   c.nx = gx.nd; c.ny = gy.nd;
   c.lox = gx.lo; c.loy = gy.lo;
   c.ldn = (gy.nd + 3) & ~3;
-  // bf16-split factors: a column stride of 4 (mod 8) complex values keeps the
-  // four columns of an mma A fragment in distinct shared-memory banks
-  if (split) {
+  // complex64 and bf16-split factors: a column stride of 4 (mod 8) complex
+  // values keeps the four columns of an mma A fragment in distinct
+  // shared-memory banks
+  if (fp32_factors) {
     c.ldn = gy.nd;
     while (c.ldn % 8 != 4) ++c.ldn;
   }
@@ -300,7 +302,7 @@ void tune_file_append(const std::string& key, const TuneEntry& e) {
   FILE* f = std::fopen(path, "a");
   if (!f) return;
   std::fprintf(f, "%s", key.c_str());
-  for (size_t i = 0; i < e.r.size(); ++i) std::fprintf(f, " %d,%d,%.5f", e.r[i], e.cl[i], e.ms[i]);
+  for (size_t i = 0; i < e.r.size(); ++i) std::fprintf(f, " %d,%d,%.9g", e.r[i], e.cl[i], e.ms[i]);
   std::fprintf(f, "\n");
   std::fclose(f);
 }
@@ -348,14 +350,21 @@ lsw_status tune_fronts(lsw_ctx* ctx, int nrhs, const FrontPlan& plan, cudaStream
         if (hit != seen[fi].end()) {
           ms = hit->second;
         } else {
-          if ((s = launch_front_of(ctx, &sc, fi, st)) != LSW_OK) break;
-          if (cudaEventRecord(e0, st) != cudaSuccess) { s = fail(ctx, LSW_ERR_CUDA, "event"); break; }
-          if ((s = launch_front_of(ctx, &sc, fi, st)) != LSW_OK) break;
-          if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
-              cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
-            s = fail(ctx, LSW_ERR_CUDA, "timing a sweep-front shape");
-            break;
+          // timed once; a short launch (where a first launch's overheads
+          // would show) is timed a second time and the smaller time kept
+          for (int rep = 0; rep < 2 && s == LSW_OK; ++rep) {
+            float t = 0.f;
+            if (cudaEventRecord(e0, st) != cudaSuccess) { s = fail(ctx, LSW_ERR_CUDA, "event"); break; }
+            if ((s = launch_front_of(ctx, &sc, fi, st)) != LSW_OK) break;
+            if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                cudaEventElapsedTime(&t, e0, e1) != cudaSuccess) {
+              s = fail(ctx, LSW_ERR_CUDA, "timing a sweep-front shape");
+              break;
+            }
+            ms = rep == 0 ? t : std::min(ms, t);
+            if (t > 2.0f) break;
           }
+          if (s != LSW_OK) break;
           seen[fi][shape] = ms;
         }
         if (ms < out->ms[fi] * 0.99f) { out->ms[fi] = ms; out->r[fi] = r; out->cl[fi] = cl; }
@@ -383,7 +392,10 @@ lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out, cudaStream_t st)
       return fail(ctx, LSW_ERR_UNSUPPORTED, ex.what());
     }
     TuneEntry tuned;
-    if (ctx->tune && ctx->factorized) {
+    if (ctx->force_r > 0) {
+      plan.forced_r.assign(8 * (size_t)ctx->N + 8, ctx->force_r);
+      plan.forced_cl.assign(8 * (size_t)ctx->N + 8, ctx->force_cl);
+    } else if (ctx->tune && ctx->factorized) {
       std::lock_guard<std::mutex> lk(g_tune_mu);
       tune_file_read();
       const std::string key = tune_key(ctx, nrhs);
@@ -664,6 +676,15 @@ lsw_status lsw_ctx_create(lsw_ctx** out, int device) {
   if (const char* ev = std::getenv("LSW_FACTOR_TC")) c->factor_tc = std::atoi(ev) != 0;
   // LSW_TUNE=0 leaves every sweep-front shape to the cost model
   if (const char* ev = std::getenv("LSW_TUNE")) c->tune = std::atoi(ev) != 0;
+  // LSW_FRONT_SHAPE=RxC imposes R slots per item (4, 8, 16) and C CTAs per half
+  // chain (1, 2, 4) on every sweep front where that shape fits (no tuning)
+  if (const char* ev = std::getenv("LSW_FRONT_SHAPE")) {
+    int r = 0, cl = 0;
+    if (std::sscanf(ev, "%dx%d", &r, &cl) == 2 && (r == 4 || r == 8 || r == 16) && (cl == 1 || cl == 2 || cl == 4)) {
+      c->force_r = r;
+      c->force_cl = cl;
+    }
+  }
   {
     cudaDeviceProp prop{};
     if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) {
@@ -801,7 +822,7 @@ lsw_status lsw_problem_setup(lsw_ctx* ctx, const lsw_geom* g, const double* m_gr
   ctx->max_nx = ctx->max_ny = 0;
   for (int I = 0; I < ctx->N; ++I)
     for (int J = 0; J < ctx->N; ++J) {
-      DevCell c = make_cell(I, J, ctx->N, ctx->m, ctx->p, precision == LSW_PREC_SPLIT);
+      DevCell c = make_cell(I, J, ctx->N, ctx->m, ctx->p, precision != LSW_PREC_C128);
       c.fac_off = fac_off;
       fac_off += (long long)c.nx * c.ny * c.ldn;
       c.prof_off = (long long)prof.size();

@@ -19,16 +19,22 @@
 //     and a second one the scaled pivot row (double-buffered by step parity).
 //     It records f_t (column t at step t), the pivots p_t and 1 / f_t[p_t].
 //   * Every other column then receives the B steps at once.  With
-//     u = M1 g (g the pivot rows, M1 = (D + L)^-1 of the pivots' f values) the
-//     whole block -- the rank-B update of the other rows and the final values
-//     of the pivot rows -- is one product:
-//         W[r][c] -= sum_t F'_t[r] u_t[c],   F'_t[r] = f_t[r] - [r == p_t],
-//     issued as tcgen05.mma kind::tf32 from shared-memory operand tiles into
-//     the TMEM accumulator: the complex product as a real one (A = [Re F' |
-//     Im F'] interleaved along k, B holding (Re u, -Im u) and (Im u, Re u)
-//     per output column pair), each FP32 operand split into TF32 hi + lo and
-//     three products hi*hi + hi*lo + lo*hi accumulated in FP32 (about 21
-//     significant bits per product).  The panel's own columns get u = 0.
+//     u = M1 g (g the pivot rows, M1 = (D + L)^-1 of the pivots' f values)
+//     the rank-B update of the rows that are not pivots of the block is one
+//     product:
+//         W[r][c] -= sum_t f_t[r] u_t[c],
+//     issued as tcgen05.mma kind::f16 from shared-memory operand tiles into
+//     the TMEM accumulator: the complex product as a real one (A = [Re f |
+//     Im f] interleaved along k, B holding (Re u, -Im u) and (Im u, Re u)
+//     per output column pair), each FP32 operand split into three bf16 terms
+//     (hi + mid + lo, 24 significant bits) and the six products whose terms
+//     reach 2^-16 accumulated in FP32 (the neglected ones are below 2^-23 of
+//     the product).  The pivot rows of the block take the MMA with zero A
+//     rows and get their final values c[p_t] = u_t - sum_{s>t} f_s[p_t] u_s
+//     on the CUDA cores afterwards: written as one product with the pivot
+//     rows included, W[p_t] - sum f u + u_t would cancel terms of the size of
+//     the matrix entries (1/h^2) down to the size of the inverse's (h^2).
+//     The panel's own columns get u = 0.
 //   * Unscrambled column-major into the factor pool through a shared-memory
 //     staging tile (Sinv[i][j] = W[piv[i]][pinv[j]]).
 // A thread-block cluster of G CTAs (G = 2 for cells of 97-192 DOFs per side)
@@ -56,13 +62,14 @@ constexpr unsigned kTmemCols = 512;
 constexpr unsigned kSuspendNs = 1000000;
 
 // shared layout (bytes)
-constexpr int kOffAhi = 0;                          // [256 rows][32 k] tf32, canonical K-major
-constexpr int kOffAlo = 32768;
-constexpr int kOffBhi = 65536;                      // [192 rows][32 k]
-constexpr int kOffBlo = 65536 + 24576;
-constexpr int kOffF = 114688;                       // float2 [2][kB][kMaxRows]
+constexpr int kATerm = 16384;                       // [256 rows][32 k] bf16, canonical K-major: one split term
+constexpr int kBTerm = 12288;                       // [192 rows][32 k] bf16
+constexpr int kOffA = 0;                            // three terms: hi, mid, lo
+constexpr int kOffB = 3 * kATerm;
+constexpr int kOffF = kOffB + 3 * kBTerm;           // float2 [2][kB][kMaxRows]
 constexpr int kOffGU = kOffF + 2 * kB * kMaxRows * 8;              // float2 [kB][kMaxCols]
-constexpr int kOffRB = kOffGU + kB * kMaxCols * 8;                 // float2 [2][kB + 1]
+constexpr int kOffU = kOffGU + kB * kMaxCols * 8;                  // float2 [kB][kMaxCols]
+constexpr int kOffRB = kOffU + kB * kMaxCols * 8;                  // float2 [2][kB + 1]
 constexpr int kOffInv = kOffRB + 2 * (kB + 1) * 8;                 // float2 [2][kB]
 constexpr int kOffM1 = kOffInv + 2 * kB * 8;                       // float2 [kB][kB]
 constexpr int kOffInts = kOffM1 + kB * kB * 8;                     // used, piv, pslot, pinv [kMaxRows] each
@@ -71,7 +78,8 @@ constexpr int kOffKey = kOffPb + 2 * kB * 4;                       // unsigned [
 constexpr int kOffBar = kOffKey + 64;                              // 3 mbarriers
 constexpr int kOffMisc = kOffBar + 24;                             // abort flag, TMEM address
 constexpr int kSmem = kOffMisc + 16;
-static_assert(kOffF == kOffBlo + 24576, "layout");
+static_assert(kOffF == 86016, "layout");
+static_assert(16 * kMaxRows * 8 <= 3 * kATerm, "unscramble staging tile [16][ldn] fits in the A operand area");
 static_assert(kOffBar % 8 == 0, "mbarrier alignment");
 
 __device__ __forceinline__ unsigned saddr(const void* p) {
@@ -118,16 +126,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity) {
       : "memory");
   return ok != 0;
 }
-__device__ __forceinline__ float2 ld_remote(const float2* p, unsigned rank) {
-  float2 v;
-  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(mapa(saddr(p), rank))
+// stores into CTA `rank`'s shared memory at the offset of p (ordered for the
+// peer by the cluster barrier that follows)
+__device__ __forceinline__ void st_remote(float2* p, unsigned rank, float2 v) {
+  asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(mapa(saddr(p), rank)), "f"(v.x), "f"(v.y)
                : "memory");
-  return v;
 }
-__device__ __forceinline__ int ld_remote(const int* p, unsigned rank) {
-  int v;
-  asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(mapa(saddr(p), rank)) : "memory");
-  return v;
+__device__ __forceinline__ void st_remote(int* p, unsigned rank, int v) {
+  asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(mapa(saddr(p), rank)), "r"(v) : "memory");
 }
 __device__ __forceinline__ void named_sync(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
@@ -170,32 +176,37 @@ __device__ __forceinline__ void tm_st32(unsigned taddr, const float (&v)[32]) {
 }
 __device__ __forceinline__ void tm_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
-__device__ __forceinline__ float tf32_rn(float x) {
-  unsigned r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
-}
-// byte offset of element (row, k) in a [rows x 32] tf32 tile in the canonical
-// K-major layout without swizzle: 8-row x 16-byte core matrices, k-adjacent
-// core matrices 128 B apart (leading-dimension offset), 8-row groups 1024 B
-// apart (stride-dimension offset)
+// byte offset of element (row, k) in a [rows x 32] bf16 tile in the canonical
+// K-major layout without swizzle: 8-row x 16-byte core matrices (8 k each),
+// k-adjacent core matrices 128 B apart (leading-dimension offset), 8-row
+// groups 512 B apart (stride-dimension offset)
 __device__ __forceinline__ int kmaj(int row, int k) {
-  return (row >> 3) * 1024 + (k >> 2) * 128 + (row & 7) * 16 + (k & 3) * 4;
+  return (row >> 3) * 512 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
 }
 // shared-memory matrix descriptor (tcgen05 format: start, leading and stride
 // byte offsets in 16-byte units, version 1, no swizzle)
 __device__ __forceinline__ uint64_t sdesc(unsigned addr) {
-  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(1024u >> 4) << 32) |
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(512u >> 4) << 32) |
          (1ull << 46);
 }
-__device__ __forceinline__ void put_split(unsigned char* hi, unsigned char* lo, int off, float x) {
-  const float h = tf32_rn(x);
-  *reinterpret_cast<float*>(hi + off) = h;
-  *reinterpret_cast<float*>(lo + off) = tf32_rn(x - h);
+// (a, b) as three bf16x2 terms hi + mid + lo (each the rounded remainder of
+// the previous ones; the remainders are exact in FP32), a in the low half, at
+// byte offset `off` (4-byte aligned: k even) of the three term tiles `term`
+// bytes apart
+__device__ __forceinline__ void put3(unsigned char* base, int term, int off, float a, float b) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  const float ra = a - __low2float(h), rb = b - __high2float(h);
+  const __nv_bfloat162 m = __floats2bfloat162_rn(ra, rb);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(ra - __low2float(m), rb - __high2float(m));
+  *reinterpret_cast<__nv_bfloat162*>(base + off) = h;
+  *reinterpret_cast<__nv_bfloat162*>(base + term + off) = m;
+  *reinterpret_cast<__nv_bfloat162*>(base + 2 * term + off) = l;
 }
-__device__ __forceinline__ void mma_tf32(unsigned d, uint64_t a, uint64_t b, unsigned idesc) {
+// D (TMEM, FP32) += A B with A, B bf16 from shared memory (A negated by the
+// instruction descriptor)
+__device__ __forceinline__ void mma_bf16(unsigned d, uint64_t a, uint64_t b, unsigned idesc) {
   asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, 1, 0;\n\ttcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, 1, 0;\n\ttcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(
           d),
       "l"(a), "l"(b), "r"(idesc)
       : "memory");
@@ -242,12 +253,11 @@ k_factorize_tc(const DevCell* __restrict__ cells, const double2* __restrict__ pr
   const bool live = r < n;
   const bool warp_rows = 32 * warp < n;               // my warp holds a row of the matrix
 
-  unsigned char* Ahi = smem + kOffAhi;
-  unsigned char* Alo = smem + kOffAlo;
-  unsigned char* Bhi = smem + kOffBhi;
-  unsigned char* Blo = smem + kOffBlo;
+  unsigned char* Aop = smem + kOffA;
+  unsigned char* Bop = smem + kOffB;
   C* F = reinterpret_cast<C*>(smem + kOffF);          // [2][kB][kMaxRows]
-  C* GU = reinterpret_cast<C*>(smem + kOffGU);        // [kB][kMaxCols] pivot rows g
+  C* GU = reinterpret_cast<C*>(smem + kOffGU);        // [kB][kMaxCols] pivot rows g, then their final values
+  C* U = reinterpret_cast<C*>(smem + kOffU);          // [kB][kMaxCols] u = M1 g
   C* RB = reinterpret_cast<C*>(smem + kOffRB);        // [2][kB + 1] scaled pivot row, 1/pivot last
   C* invv = reinterpret_cast<C*>(smem + kOffInv);     // [2][kB]
   C* M1 = reinterpret_cast<C*>(smem + kOffM1);        // [kB][kB]
@@ -365,9 +375,9 @@ k_factorize_tc(const DevCell* __restrict__ cells, const double2* __restrict__ pr
                                 : "memory");
   };
 
-  // instruction descriptor: D FP32, A and B TF32, A negated (D -= A B), both
+  // instruction descriptor: D FP32, A and B bf16, A negated (D -= A B), both
   // K-major, N = NP, M = 128
-  const unsigned idesc = (1u << 4) | (2u << 7) | (2u << 10) | (1u << 13) | ((unsigned)(NP >> 3) << 17) |
+  const unsigned idesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 13) | ((unsigned)(NP >> 3) << 17) |
                          ((unsigned)(128 >> 4) << 24);
 
   for (int step = 0; step < nsteps; ++step) {
@@ -444,7 +454,11 @@ k_factorize_tc(const DevCell* __restrict__ cells, const double2* __restrict__ pr
           if (t >= bt) break;
           const int par = t & 1;
           const C v = row[t];
-          if (live) Fb_[(size_t)t * kMaxRows + r] = v;
+          if (live) {
+            Fb_[(size_t)t * kMaxRows + r] = v;
+            for (int q = 0; q < G; ++q)
+              if (q != (int)g) st_remote(Fb_ + (size_t)t * kMaxRows + r, (unsigned)q, v);
+          }
           // pivot key: |v|^2 as float bits (monotone for non-negative values) with
           // the low byte replaced by 255 - row: the largest magnitude, ties (to
           // 2^-15) to the lowest row; pivoted rows have key 0
@@ -471,6 +485,11 @@ k_factorize_tc(const DevCell* __restrict__ cells, const double2* __restrict__ pr
             piv[k0 + t] = r;
             pbb[t] = r;
             ivb[t] = inv;
+            for (int q = 0; q < G; ++q)
+              if (q != (int)g) {
+                st_remote(pbb + t, (unsigned)q, r);
+                st_remote(ivb + t, (unsigned)q, inv);
+              }
 #pragma unroll
             for (int q = 0; q < kB; ++q)
               if (q < bt) {
@@ -509,22 +528,15 @@ k_factorize_tc(const DevCell* __restrict__ cells, const double2* __restrict__ pr
         }
       }
       if (!csync()) { leave(); return; }
-      if ((int)g != o) {
-        // the panel owner's columns f_t, pivots and reciprocals
-        for (int e = tid; e < bt * n; e += kT) {
-          const int t = e / n, rr = e - t * n;
-          Fb_[(size_t)t * kMaxRows + rr] = ld_remote(Fb_ + (size_t)t * kMaxRows + rr, (unsigned)o);
-        }
-        if (tid < bt) {
-          const int p = ld_remote(pbb + tid, (unsigned)o);
-          pbb[tid] = p;
-          ivb[tid] = ld_remote(ivb + tid, (unsigned)o);
-          used[p] = 1;
-          piv[k0 + tid] = p;
-        }
-        __syncthreads();
+      // the panel owner pushed f_t, the pivots and the reciprocals into every
+      // CTA's buffers before the cluster barrier
+      if ((int)g != o && tid < bt) {
+        const int p = pbb[tid];
+        used[p] = 1;
+        piv[k0 + tid] = p;
       }
       if (tid < bt) pslot[pbb[tid]] = tid;
+      __syncthreads();
       // M1 = (D + L)^-1 (D = diag f_t[p_t], L[t][s] = f_s[p_t], s < t), one warp,
       // lane j solving for column j
       if (warp == 0 && lane < bt) {
@@ -541,19 +553,17 @@ k_factorize_tc(const DevCell* __restrict__ cells, const double2* __restrict__ pr
           }
         }
       }
-      // A operand: F'_t[r] = f_t[r] - [r == p_t] as (Re, Im) along k, hi / lo
+      // A operand: f_t[r] as (Re, Im) along k, three bf16 terms; zero rows for
+      // the block's pivot rows (finished on the CUDA cores after the product)
       if (r < 128 * ntiles) {
+        const bool is_piv = live && pslot[r] >= 0;
+#pragma unroll
         for (int t = 0; t < kB; ++t) {
           C f = z;
-          if (live && t < bt) {
-            f = Fb_[(size_t)t * kMaxRows + r];
-            if (r == pbb[t]) f.x -= 1.f;
-          }
-          put_split(Ahi, Alo, kmaj(r, 2 * t), f.x);
-          put_split(Ahi, Alo, kmaj(r, 2 * t + 1), f.y);
+          if (live && t < bt && !is_piv) f = Fb_[(size_t)t * kMaxRows + r];
+          put3(Aop, kATerm, kmaj(r, 2 * t), f.x, f.y);
         }
       }
-      __syncthreads();
       // g: the pivot rows of my columns, from the warps that hold them
       {
         const bool has = __any_sync(0xffffffffu, live && pslot[r] >= 0);
@@ -571,54 +581,93 @@ k_factorize_tc(const DevCell* __restrict__ cells, const double2* __restrict__ pr
         }
       }
       __syncthreads();
-      // u = M1 g per column; B operand rows 2c: (Re u, -Im u), 2c + 1: (Im u, Re u)
-      // along k = (2t, 2t + 1); the panel's own columns and the padding get u = 0
-      if (2 * tid < NP) {
-        const int cc = tid;
-        C u[kB];
-        const bool panel_col = (int)g == o && cc >= k0 - c0 && cc < k1 - c0;
-#pragma unroll
-        for (int t = 0; t < kB; ++t) {
-          C a = z;
-          if (t < bt && cc < nc && !panel_col) {
-#pragma unroll
-            for (int s2 = 0; s2 < kB; ++s2)
-              if (s2 <= t) cfma(a, M1[t * kB + s2], GU[(size_t)s2 * kMaxCols + cc]);
-          }
-          u[t] = a;
-        }
-#pragma unroll
-        for (int t = 0; t < kB; ++t) {
-          put_split(Bhi, Blo, kmaj(2 * cc, 2 * t), u[t].x);
-          put_split(Bhi, Blo, kmaj(2 * cc, 2 * t + 1), -u[t].y);
-          put_split(Bhi, Blo, kmaj(2 * cc + 1, 2 * t), u[t].y);
-          put_split(Bhi, Blo, kmaj(2 * cc + 1, 2 * t + 1), u[t].x);
-        }
+      // u = M1 g per (pivot, column); the panel's own columns and pivots past
+      // the block get u = 0
+      const int pcol0 = (int)g == o ? k0 - c0 : nc, pcol1 = (int)g == o ? k1 - c0 : nc;
+      for (int e = tid; e < kB * nc; e += kT) {
+        const int t = e / nc, cc = e - t * nc;
+        C a = z;
+        if (t < bt && (cc < pcol0 || cc >= pcol1))
+          for (int s2 = 0; s2 <= t; ++s2) cfma(a, M1[t * kB + s2], GU[(size_t)s2 * kMaxCols + cc]);
+        U[(size_t)t * kMaxCols + cc] = a;
+      }
+      __syncthreads();
+      // B operand rows 2c: (Re u, -Im u), 2c + 1: (Im u, Re u) along k = (2t,
+      // 2t + 1); the padding columns get zeros
+      for (int e = tid; e < kB * (NP / 2); e += kT) {
+        const int t = e / (NP / 2), cc = e - t * (NP / 2);
+        const C u = cc < nc ? U[(size_t)t * kMaxCols + cc] : z;
+        put3(Bop, kBTerm, kmaj(2 * cc, 2 * t), u.x, -u.y);
+        put3(Bop, kBTerm, kmaj(2 * cc + 1, 2 * t), u.y, u.x);
       }
       // operand writes (generic proxy) visible to the tensor core (async proxy)
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       tc_fence_before();
       __syncthreads();
       tc_fence_after();
-      // ---- the block's update on the tensor cores: W -= F' U, 3 x TF32 ----
+      // ---- the block's update on the tensor cores: W -= F U, bf16 x 3 ----
+      // (A term i, B term j) for i + j <= 2: hi hi, hi mid, mid hi, hi lo,
+      // mid mid, lo hi; two k-steps of 16 per 128-row tile
       if (tid == 0) {
-        const unsigned ah = saddr(Ahi), al = saddr(Alo), bh = saddr(Bhi), bl = saddr(Blo);
+        const unsigned a0 = saddr(Aop), b0 = saddr(Bop);
         for (int tile = 0; tile < ntiles; ++tile) {
           const unsigned d = tbase + (unsigned)(256 * tile);
-          const unsigned ao = (unsigned)tile * 16384u;
+          const unsigned ao = (unsigned)tile * 8192u;
 #pragma unroll
-          for (int s = 0; s < 4; ++s) {
+          for (int s = 0; s < 2; ++s) {
             const unsigned ko = (unsigned)s * 256u;
-            mma_tf32(d, sdesc(ah + ao + ko), sdesc(bh + ko), idesc);
-            mma_tf32(d, sdesc(ah + ao + ko), sdesc(bl + ko), idesc);
-            mma_tf32(d, sdesc(al + ao + ko), sdesc(bh + ko), idesc);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+              for (int j = 0; j + i < 3; ++j)
+                mma_bf16(d, sdesc(a0 + (unsigned)(i * kATerm) + ao + ko), sdesc(b0 + (unsigned)(j * kBTerm) + ko),
+                         idesc);
           }
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(mmabar))
                      : "memory");
       }
       mma_pending = true;
+      // while the tensor cores run: the block's pivot rows, which the product
+      // leaves as they were, c[p_t] = u_t - sum_{s>t} f_s[p_t] u_s on my columns
+      // outside the panel, into GU
+      for (int e = tid; e < bt * nc; e += kT) {
+        const int t = e / nc, cc = e - t * nc;
+        C a = U[(size_t)t * kMaxCols + cc];
+        const int pt = pbb[t];
+        for (int s2 = t + 1; s2 < bt; ++s2) cfms(a, Fb_[(size_t)s2 * kMaxRows + pt], U[(size_t)s2 * kMaxCols + cc]);
+        GU[(size_t)t * kMaxCols + cc] = a;
+      }
+      __syncthreads();
       if (!wait_mma(true)) { leave(); return; }
+      tc_fence_after();
+      // the pivot rows' final values into TMEM (the panel's columns keep the
+      // panel's values)
+      {
+        const int sl = live ? pslot[r] : -1;
+        const bool has = __any_sync(0xffffffffu, sl >= 0);
+        if (warp_rows && has) {
+          for (int cb = 0; cb < nc; cb += 16) {
+            float v[32];
+            tm_ld32(trow + 2 * cb, v);
+            if (sl >= 0) {
+#pragma unroll
+              for (int q = 0; q < 16; ++q) {
+                const int cc = cb + q;
+                if (cc < nc && (cc < pcol0 || cc >= pcol1)) {
+                  const C a = GU[(size_t)sl * kMaxCols + cc];
+                  v[2 * q] = a.x;
+                  v[2 * q + 1] = a.y;
+                }
+              }
+            }
+            tm_st32(trow + 2 * cb, v);
+          }
+          tm_wait_st();
+        }
+      }
+      tc_fence_before();
+      __syncthreads();
       tc_fence_after();
       if (tid < bt) pslot[pbb[tid]] = -1;
       __syncthreads();
@@ -630,7 +679,7 @@ k_factorize_tc(const DevCell* __restrict__ cells, const double2* __restrict__ pr
     // area (16 columns at a time) ----
     for (int i = tid; i < n; i += kT) pinv[piv[i]] = i;
     __syncthreads();
-    C* stg = reinterpret_cast<C*>(smem + kOffAhi);   // [16][ldn]
+    C* stg = reinterpret_cast<C*>(smem + kOffA);     // [16][ldn]
     C* Fk = Fac + (size_t)k * n * ldn;
     for (int cb = 0; cb < nc; cb += 16) {
       if (warp_rows) {
