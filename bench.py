@@ -496,7 +496,10 @@ def run_serve(args):
     for i, rate in enumerate(rates):
         # every rate starts from an empty factor cache with its own stream
         eng = ServeEngine(GpuBackend(0), slots=args.serve_slots, max_batch=8)
-        reqs = serving_stream(args.serve_requests, rate_hz=rate, seed=3 + i)
+        # --serve-window caps the stream by time: the requests of that many
+        # seconds of Poisson arrivals at this rate
+        n_req = max(1, int(round(rate * args.serve_window))) if args.serve_window > 0 else args.serve_requests
+        reqs = serving_stream(n_req, rate_hz=rate, seed=3 + i)
         st = eng.run(reqs, realtime=True)
         res = [r.true_rel_res for r in reqs if r.error is None]
         print(json.dumps({"metric": "serving: p50/p99 latency and solves/s at rel. residual 1e-6",
@@ -526,6 +529,8 @@ def main():
     ap.add_argument("--serve", action="store_true", help="serving stream at the rates of --serve-rates")
     ap.add_argument("--serve-rates", default="1,4,16")
     ap.add_argument("--serve-requests", type=int, default=40)
+    ap.add_argument("--serve-window", type=float, default=0.0,
+                    help="seconds of arrivals per rate (overrides --serve-requests when > 0)")
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--config", default="C4")
     ap.add_argument("--precision", default=None, choices=["c64", "bf16x2", "c128"],
