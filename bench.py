@@ -384,11 +384,14 @@ def run_gpu(args):
     }
     peak, peak_kind = measured_peaks()
     achieved = pr["alg_bytes"] / (front_ms / 1e3) / 1e9
+    # DRAM traffic of the fronts: the ncu capture's traffic per algorithmic
+    # byte (a full C2 apply of the same kernel and precision) times this
+    # apply's algorithmic bytes
     traffic = None
-    tf = ROOT / "profiles" / "k_front_C2_dram_traffic.md"
-    if tf.exists() and args.config.upper() == "C2" and nrhs == 1:
-        m = re.search(r"traffic_bytes_per_apply_c2:\s*([0-9.eE+]+)", tf.read_text())
-        traffic = float(m.group(1)) if m else None
+    tf = ROOT / "profiles" / "k_front_dram_traffic.md"
+    if tf.exists() and prec in ("c64", "bf16x2"):
+        m = re.search(r"traffic_per_alg_byte_%s:\s*([0-9.eE+]+)" % prec, tf.read_text())
+        traffic = float(m.group(1)) * pr["alg_bytes"] if m else None
 
     # plain FP64 GPU path
     S64 = None
@@ -449,6 +452,9 @@ def run_gpu(args):
             if fp64 else None,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak if peak else None, "traffic": traffic,
+                         "traffic_source": "ncu DRAM bytes per algorithmic byte of a full C2 apply of this kernel "
+                                           "and precision (profiles/k_front_dram_traffic.md), times this apply's "
+                                           "algorithmic bytes" if traffic else None,
                          "kernel": "k_front (sweep-front cell solves), all fronts of one apply",
                          "peak_kind": peak_kind, "alg_bytes_per_apply": pr["alg_bytes"],
                          "streamed_bytes_per_apply": pr["streamed_bytes"],
@@ -481,8 +487,13 @@ def run_apply_only(args):
     for _ in range(args.warmup + args.steps):
         S.apply_precond(v)
     torch.cuda.synchronize()
-    print(json.dumps({"apply_only": args.config, "precision": prec, "nrhs": args.nrhs,
-                      "applies": args.warmup + args.steps, "fronts_per_apply": 3 * spec.N - 3 + 1}))
+    line = {"apply_only": args.config, "precision": prec, "nrhs": args.nrhs,
+            "applies": args.warmup + args.steps, "fronts_per_apply": 3 * spec.N - 3 + 1}
+    if args.warmup + args.steps > 0:
+        # the algorithmic and streamed bytes of one apply (one more, profiled, apply)
+        _, pr = S.apply_precond_profiled(v)
+        line.update({k: pr[k] for k in ("alg_bytes", "streamed_bytes", "front_ms", "fronts", "items")})
+    print(json.dumps(line))
 
 
 def run_serve(args):

@@ -140,17 +140,16 @@ lsw_status cuda_fail(lsw_ctx* c, cudaError_t e, const char* where) {
 inline size_t csize(int prec) { return prec == LSW_PREC_C128 ? 16 : 8; }
 inline cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
-DevCell make_cell(int I, int J, int N, int m, int p, bool fp32_factors) {
+DevCell make_cell(int I, int J, int N, int m, int p, bool split) {
   DevCell c{};
   const DirGeom gx = dir_geom(J, N, m, p), gy = dir_geom(I, N, m, p);
   c.I = I; c.J = J;
   c.nx = gx.nd; c.ny = gy.nd;
   c.lox = gx.lo; c.loy = gy.lo;
   c.ldn = (gy.nd + 3) & ~3;
-  // complex64 and bf16-split factors: a column stride of 4 (mod 8) complex
-  // values keeps the four columns of an mma A fragment in distinct
-  // shared-memory banks
-  if (fp32_factors) {
+  // bf16-split factors: a column stride of 4 (mod 8) complex values keeps the
+  // four columns of an mma A fragment in distinct shared-memory banks
+  if (split) {
     c.ldn = gy.nd;
     while (c.ldn % 8 != 4) ++c.ldn;
   }
@@ -822,7 +821,7 @@ lsw_status lsw_problem_setup(lsw_ctx* ctx, const lsw_geom* g, const double* m_gr
   ctx->max_nx = ctx->max_ny = 0;
   for (int I = 0; I < ctx->N; ++I)
     for (int J = 0; J < ctx->N; ++J) {
-      DevCell c = make_cell(I, J, ctx->N, ctx->m, ctx->p, precision != LSW_PREC_C128);
+      DevCell c = make_cell(I, J, ctx->N, ctx->m, ctx->p, precision == LSW_PREC_SPLIT);
       c.fac_off = fac_off;
       fac_off += (long long)c.nx * c.ny * c.ldn;
       c.prof_off = (long long)prof.size();

@@ -208,19 +208,6 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], unsigned a0, unsigned a1
                : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
                : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
-// D += A B, m16n8k8, tf32 operands, FP32 accumulation
-__device__ __forceinline__ void mma_tf32(float (&d)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
-                                         unsigned b0, unsigned b1) {
-  asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-               "{%0,%1,%2,%3};"
-               : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-               : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-// x as tf32 hi + lo terms: hi = rn_tf32(x), lo = rn_tf32(x - hi) (x - hi exact in FP32)
-__device__ __forceinline__ void tf32_split(float x, unsigned& hi, unsigned& lo) {
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(x));
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lo) : "f"(x - __uint_as_float(hi)));
-}
 
 // CTA c of a cluster of CL owns rows/columns [c*ny/CL, (c+1)*ny/CL)
 __device__ __forceinline__ int owner_of(int row, int ny, int CL) { return ((row + 1) * CL - 1) / ny; }
@@ -305,18 +292,9 @@ template <> struct Pair<double> {
   __device__ __forceinline__ void load(const double2* p) { a = p[0]; b = p[1]; }
 };
 
-// The matvec of a line: complex FMAs on the CUDA cores (kFma), bf16 hi/lo
-// factor terms on the tensor cores (kSplit), or complex64 factors on the
-// tensor cores as three tf32 products of hi/lo terms (kTf32).
-enum : int { kFma = 0, kSplit = 1, kTf32 = 2 };
-
-template <typename T, int R, int MODE>
+template <typename T, int R, bool SPLIT>
 __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it, const DevCell& cl, unsigned char* smem) {
   using C = cx_t<T>;
-  constexpr bool SPLIT = MODE == kSplit;
-  constexpr bool TF = MODE == kTf32;
-  constexpr bool MMA = MODE != kFma;
-  constexpr int BWW = TF ? 2 : 1;      // 32-bit words per staged B entry (tf32: the Re-k and Im-k values)
   const int CW = a.chunk;              // columns per chunk, multiple of 8
   const int KSW = a.ksw;               // column slices: consumer warps per row group
   static_assert((2 * kNSMax + 4) * 8 + 4 <= kHdr, "barrier header");
@@ -351,7 +329,7 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   const int nJ = je - jb;               // my columns / rows of every line
   const int RG = (ny + 63) >> 6;        // row groups of 64 rows
   // consumer warps: KSW column slices per row group, or (split) one per 16-row m-tile
-  const int NCW = MMA ? (ny + 15) >> 4 : KSW * RG;
+  const int NCW = SPLIT ? (ny + 15) >> 4 : KSW * RG;
   constexpr int NT = (2 * R + 7) / 8;   // split: n-tiles of 8 (Re, Im interleaved per slot)
   constexpr int NT8 = NT * 8;
   const int NCT = NCW * 32;
@@ -400,15 +378,13 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   const size_t qbuf = (size_t)CL * qplane;
   p = al16(p + 2 * qbuf * sizeof(C));
   C* LS = reinterpret_cast<C*>(p);      // [KSW][R][64 RG] the column slices' partial sums, before their sum
-  if (!MMA) p = al16(p + (size_t)KSW * 64 * RG * R * sizeof(C));
-  // tensor-core matvecs: the next line's input as mma B words, hi and lo
-  // terms, [column][n] with n = 2 slot + (0: real part, 1: imaginary part) of
-  // the product (tf32: two words per entry, for the factor's real and
-  // imaginary k)
+  if (!SPLIT) p = al16(p + (size_t)KSW * 64 * RG * R * sizeof(C));
+  // split: the next line's input as mma B words, hi and lo terms, [column][n]
+  // with n = 2 slot + (0: real part, 1: imaginary part) of the product
   const int nJ8 = ((nJcap + 7) & ~7) + 8;
   unsigned* BwH = reinterpret_cast<unsigned*>(p);
-  unsigned* BwL = BwH + (size_t)nJ8 * NT8 * BWW;
-  if (MMA) p = al16(p + 2 * (size_t)nJ8 * NT8 * BWW * sizeof(unsigned));
+  unsigned* BwL = BwH + (size_t)nJ8 * NT8;
+  if (SPLIT) p = al16(p + 2 * (size_t)nJ8 * NT8 * sizeof(unsigned));
   int* rowinfo = reinterpret_cast<int*>(p);   // [ny] owner CTA << 16 | row offset in the owner's range
   p = al16(p + sizeof(int) * ny);
   DevSlot* sl = reinterpret_cast<DevSlot*>(p);
@@ -465,12 +441,12 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
     wsh[k] = to_c(px[k], czero<C>());
     esh[k] = to_c(px[nx + k], czero<C>());
   }
-  if constexpr (MMA) {
+  if constexpr (SPLIT) {
     // the mma k-steps of a chunk's last columns and rows past ldn read ring
     // entries no copy wrote; zeros (with zero B words past my columns) keep
     // them finite and without effect
     for (size_t i = tid; i < (size_t)NS * slot_elems; i += blockDim.x) ring[i] = czero<C>();
-    for (size_t i = tid; i < 2 * (size_t)nJ8 * NT8 * BWW; i += blockDim.x) BwH[i] = 0u;
+    for (size_t i = tid; i < 2 * (size_t)nJ8 * NT8; i += blockDim.x) BwH[i] = 0u;
   }
   if (tid == 0) {
     *abort_flag = 0;
@@ -683,21 +659,6 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
       BwL[(size_t)jj * NT8 + 2 * r] = l0;
       BwH[(size_t)jj * NT8 + 2 * r + 1] = h1;
       BwL[(size_t)jj * NT8 + 2 * r + 1] = l1;
-    } else if constexpr (TF) {
-      // k = (column, Re factor): (Re v | Im v), k = (column, Im factor): (-Im v | Re v)
-      // for output n = 2 slot | 2 slot + 1
-      const int jj = e / R, r = e - jj * R;
-      uint2 h0, l0, h1, l1;
-      tf32_split(v.x, h0.x, l0.x);
-      tf32_split(-v.y, h0.y, l0.y);
-      tf32_split(v.y, h1.x, l1.x);
-      tf32_split(v.x, h1.y, l1.y);
-      uint2* H2 = reinterpret_cast<uint2*>(BwH);
-      uint2* L2 = reinterpret_cast<uint2*>(BwL);
-      H2[(size_t)jj * NT8 + 2 * r] = h0;
-      L2[(size_t)jj * NT8 + 2 * r] = l0;
-      H2[(size_t)jj * NT8 + 2 * r + 1] = h1;
-      L2[(size_t)jj * NT8 + 2 * r + 1] = l1;
     }
   };
 
@@ -722,66 +683,7 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
     // complete without this arrive)
     if (CL > 1 && ct == 0 && li + 1 < nline) mbar_expect_tx(&pready[(li + 1) & 1], line_bytes);
     C* Qb = Q + buf * qbuf;
-    if constexpr (TF) {
-      // ---- tensor-core partial products, complex64 factors: my 16-row m-tile
-      // with all my columns on mma.sync m16n8k8 tf32.  k-step of 4 columns:
-      // k = t is the real and k = t + 4 the imaginary part of column t's
-      // factor entries (A rows g, g + 8), split into tf32 hi + lo in registers;
-      // three products hi*hi + hi*lo + lo*hi per n-tile ----
-      float cacc[NT][4];
-#pragma unroll
-      for (int nt = 0; nt < NT; ++nt) cacc[nt][0] = cacc[nt][1] = cacc[nt][2] = cacc[nt][3] = 0.f;
-      const int g = lane >> 2, t = lane & 3, mb = cw * 16;
-      const uint2* H2 = reinterpret_cast<const uint2*>(BwH);
-      const uint2* L2 = reinterpret_cast<const uint2*>(BwL);
-      for (int c = 0; c < nch; ++c, ++idx) {
-        const int slot = (int)(idx % NS);
-        const bool ok = mbar_wait<false>(&full[slot], (unsigned)((idx / NS) & 1), a.err, abort_flag, a.wait_cycles);
-        const C* S = ring + (size_t)slot * slot_elems + mb + g;
-        const int c0 = c * CW;
-        const int nks = (min(CW, nJ - c0) + 3) >> 2;
-        if (ok) {
-          for (int kq = 0; kq < nks; ++kq) {
-            const C* pa = S + (size_t)(kq * 4 + t) * ldn;
-            const C e0 = pa[0], e1 = pa[8];
-            unsigned ah0, al0, ah1, al1, ah2, al2, ah3, al3;
-            tf32_split(e0.x, ah0, al0);   // (g, t): Re, row g
-            tf32_split(e1.x, ah1, al1);   // (g + 8, t)
-            tf32_split(e0.y, ah2, al2);   // (g, t + 4): Im, row g
-            tf32_split(e1.y, ah3, al3);   // (g + 8, t + 4)
-            const size_t bo = (size_t)(c0 + kq * 4 + t) * NT8 + g;
-#pragma unroll
-            for (int nt = 0; nt < NT; ++nt) {
-              const uint2 bh = H2[bo + nt * 8], bl = L2[bo + nt * 8];
-              mma_tf32(cacc[nt], ah0, ah1, ah2, ah3, bh.x, bh.y);
-              mma_tf32(cacc[nt], ah0, ah1, ah2, ah3, bl.x, bl.y);
-              mma_tf32(cacc[nt], al0, al1, al2, al3, bh.x, bh.y);
-            }
-          }
-        }
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[slot]);
-      }
-#pragma unroll
-      for (int nt = 0; nt < NT; ++nt) {
-        const int sidx = nt * 4 + t;
-        if (sidx < R) {
-#pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            const int row = mb + g + 8 * h;
-            if (row < ny) {
-              C v;
-              v.x = cacc[nt][2 * h];
-              v.y = cacc[nt][2 * h + 1];
-              const int info = rowinfo[row];
-              C* dst = Qb + ((size_t)crank * nJcap + (info & 0xffff)) * R + sidx;
-              if (CL == 1) *dst = v;
-              else st_async(dst, (unsigned)(info >> 16), v, &pready[buf]);
-            }
-          }
-        }
-      }
-    } else if constexpr (SPLIT) {
+    if constexpr (SPLIT) {
       // ---- tensor-core partial products: my 16-row m-tile with all my columns ----
       // A (factor, bf16 hi/lo words, column-major) x B (next input, [column][n])
       // on mma.sync m16n8k16: three products hi*hi + hi*lo + lo*hi per k-step
@@ -981,46 +883,33 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
 }
 
 // 16 warps (4 auxiliary + up to 3 row groups x 4 column slices) x 128 registers
-template <typename T, int MODE>
+template <typename T, bool SPLIT>
 __global__ void __maxnreg__(128) k_front(FrontArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const DevItem it = a.items[blockIdx.x / (2 * a.cluster)];
   const DevCell cl = a.cells[it.cell];
   const int n = it.slot_count;
   if constexpr (sizeof(T) == 4) {
-    if (n <= 1) front_body<T, 1, MODE>(a, it, cl, smem);
-    else if (n <= 2) front_body<T, 2, MODE>(a, it, cl, smem);
-    else if (n <= 4) front_body<T, 4, MODE>(a, it, cl, smem);
-    else if (n <= 8) front_body<T, 8, MODE>(a, it, cl, smem);
-    else if (n <= 12) front_body<T, 12, MODE>(a, it, cl, smem);
-    else front_body<T, 16, MODE>(a, it, cl, smem);
+    if (n <= 1) front_body<T, 1, SPLIT>(a, it, cl, smem);
+    else if (n <= 2) front_body<T, 2, SPLIT>(a, it, cl, smem);
+    else if (n <= 4) front_body<T, 4, SPLIT>(a, it, cl, smem);
+    else if (n <= 8) front_body<T, 8, SPLIT>(a, it, cl, smem);
+    else if (n <= 12) front_body<T, 12, SPLIT>(a, it, cl, smem);
+    else front_body<T, 16, SPLIT>(a, it, cl, smem);
   } else {
-    if (n <= 1) front_body<T, 1, MODE>(a, it, cl, smem);
-    else if (n <= 2) front_body<T, 2, MODE>(a, it, cl, smem);
-    else if (n <= 4) front_body<T, 4, MODE>(a, it, cl, smem);
-    else front_body<T, 8, MODE>(a, it, cl, smem);
+    if (n <= 1) front_body<T, 1, SPLIT>(a, it, cl, smem);
+    else if (n <= 2) front_body<T, 2, SPLIT>(a, it, cl, smem);
+    else if (n <= 4) front_body<T, 4, SPLIT>(a, it, cl, smem);
+    else front_body<T, 8, SPLIT>(a, it, cl, smem);
   }
 }
 
-// The matvec mode of a launch whose largest item has R (padded) slots:
-// complex128 on FP64 FMAs; split factors on bf16 mma; complex64 on FP32 FMAs
-// up to 4 slots and on 3 x tf32 mma from 8 (where the FMA matvec's cost
-// grows with the slots and the factor reads no longer bound it).
-constexpr int kTf32MinSlots = 8;
-int front_mode(bool dbl, bool split, int R) {
-  if (dbl) return kFma;
-  if (split) return kSplit;
-  return R >= kTf32MinSlots ? kTf32 : kFma;
-}
-
 template <typename T>
-size_t smem_need(int ldn_max, int ny_max, int nx_max, int R, int KSW, int CL, int CW, int NS, int mode) {
+size_t smem_need(int ldn_max, int ny_max, int nx_max, int R, int KSW, int CL, int CW, int NS, bool split) {
   using C = cx_t<T>;
   const int nJ = (ny_max + CL - 1) / CL + 1;
-  const size_t bww = mode == kTf32 ? 2 : 1;
-  const size_t staging = mode != kFma
-                             ? 2 * (size_t)(((nJ + 7) & ~7) + 8) * (8 * ((2 * R + 7) / 8)) * bww * sizeof(unsigned)
-                             : (size_t)KSW * 64 * kMaxRG * R * sizeof(C);
+  const size_t staging = split ? 2 * (size_t)(((nJ + 7) & ~7) + 8) * (8 * ((2 * R + 7) / 8)) * sizeof(unsigned)
+                               : (size_t)KSW * 64 * kMaxRG * R * sizeof(C);
   return kHdr + (size_t)NS * CW * ldn_max * sizeof(C) + 4 * (size_t)R * nJ * sizeof(C) + nx_max + nJ + 32 +
          2 * (size_t)CL * R * nJ * sizeof(C) + staging + 4 * (size_t)ny_max +
          2 * (size_t)nx_max * sizeof(C) +
@@ -1037,31 +926,30 @@ namespace {
 // The launch shape of a front: column slices, chunk width and ring depth for
 // R slots on clusters of 2 CL CTAs; false if nothing fits in shared memory.
 template <typename T>
-bool front_shape(int max_ny, int max_nx, int R, int CL, int mode, int maxopt, int* ldn_out, int* ksw_out,
+bool front_shape(int max_ny, int max_nx, int R, int CL, bool split, int maxopt, int* ldn_out, int* ksw_out,
                  int* cw_out, int* ns_out, size_t* smem_out) {
   int ldn = (max_ny + 3) & ~3;
-  if (sizeof(T) == 4) {   // the complex64 / split factor layout's column stride (4 mod 8)
+  if (split) {   // the split factor layout's column stride (4 mod 8)
     ldn = max_ny;
     while (ldn % 8 != 4) ++ldn;
   }
-  const bool mma = mode != kFma;
   // largest chunk (columns, multiple of 8, <= ~64 KB) and then the deepest ring that fit
   const int nJmax = (max_ny + CL - 1) / CL;
   // column slices: as many as keep >= 4 columns per slice and the slices'
   // partial-sum staging (KSW x 192 x R) within 64 KB
   int KSW = kMaxKSW;
-  while (KSW > 1 && (mma || nJmax < 4 * KSW || (size_t)KSW * 64 * kMaxRG * R * sizeof(cx_t<T>) > 65536)) --KSW;
+  while (KSW > 1 && (split || nJmax < 4 * KSW || (size_t)KSW * 64 * kMaxRG * R * sizeof(cx_t<T>) > 65536)) --KSW;
   const int cwmax = (int)std::min<size_t>(((size_t)65536 / ((size_t)ldn * sizeof(cx_t<T>))) & ~size_t(7),
                                           (size_t)((nJmax + 7) & ~7));
   int CW = std::max(8, cwmax), NS = 0;
   for (; CW >= 8; CW -= 8) {
     for (NS = 4; NS >= 2; --NS)
-      if (smem_need<T>(ldn, max_ny, max_nx, R, KSW, CL, CW, NS, mode) <= (size_t)maxopt) break;
+      if (smem_need<T>(ldn, max_ny, max_nx, R, KSW, CL, CW, NS, split) <= (size_t)maxopt) break;
     if (NS >= 2) break;
   }
   if (CW < 8) return false;
   *ldn_out = ldn; *ksw_out = KSW; *cw_out = CW; *ns_out = NS;
-  *smem_out = smem_need<T>(ldn, max_ny, max_nx, R, KSW, CL, CW, NS, mode);
+  *smem_out = smem_need<T>(ldn, max_ny, max_nx, R, KSW, CL, CW, NS, split);
   return true;
 }
 
@@ -1072,12 +960,11 @@ int front_fit_mask(bool dbl, bool split, int max_ny, int max_nx, int slots) {
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const int R = std::min(front_rpad(std::max(1, slots)), front_rmax(dbl));
-  const int mode = front_mode(dbl, split, R);
   int mask = 0, ldn, ksw, cw, ns;
   size_t smem;
   for (int cl = 1; cl <= 4; cl *= 2) {
-    const bool ok = dbl ? front_shape<double>(max_ny, max_nx, R, cl, mode, maxopt, &ldn, &ksw, &cw, &ns, &smem)
-                        : front_shape<float>(max_ny, max_nx, R, cl, mode, maxopt, &ldn, &ksw, &cw, &ns, &smem);
+    const bool ok = dbl ? front_shape<double>(max_ny, max_nx, R, cl, split, maxopt, &ldn, &ksw, &cw, &ns, &smem)
+                        : front_shape<float>(max_ny, max_nx, R, cl, split, maxopt, &ldn, &ksw, &cw, &ns, &smem);
     if (ok) mask |= 1 << cl;
   }
   return mask;
@@ -1098,8 +985,7 @@ cudaError_t launch_front(const FrontArgs& a_in, int max_ny, int max_nx, cudaStre
   cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   int ldn = 0, KSW = 0, CW = 0, NS = 0;
   size_t smem = 0;
-  const int mode = front_mode(dbl, split, R);
-  if (!front_shape<T>(max_ny, max_nx, R, a.cluster, mode, maxopt, &ldn, &KSW, &CW, &NS, &smem))
+  if (!front_shape<T>(max_ny, max_nx, R, a.cluster, split, maxopt, &ldn, &KSW, &CW, &NS, &smem))
     return cudaErrorInvalidConfiguration;
   a.ksw = KSW;
   a.stages = NS;
@@ -1115,17 +1001,16 @@ cudaError_t launch_front(const FrontArgs& a_in, int max_ny, int max_nx, cudaStre
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  void (*kern)(FrontArgs) = k_front<T, kFma>;
-  if constexpr (sizeof(T) == 4) {
-    if (mode == kSplit) kern = k_front<float, kSplit>;
-    else if (mode == kTf32) kern = k_front<float, kTf32>;
-  }
+  auto kern = split ? k_front<float, true> : k_front<T, false>;
   // the attribute is an upper bound: always the device maximum, so that
   // host threads launching concurrently never lower it under one another
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
   if (e != cudaSuccess) return e;
   cfg.blockDim = dim3(32 * (kAux + kMaxRG * kMaxKSW));
-  return cudaLaunchKernelEx(&cfg, kern, a);
+  if constexpr (sizeof(T) == 4) {
+    if (split) return cudaLaunchKernelEx(&cfg, k_front<float, true>, a);
+  }
+  return cudaLaunchKernelEx(&cfg, k_front<T, false>, a);
 }
 
 int front_max_clusters(bool dbl, int cluster) {
@@ -1146,13 +1031,12 @@ int front_max_clusters(bool dbl, int cluster) {
   int n = 0;
   cudaError_t e;
   if (dbl) {
-    cudaFuncSetAttribute(k_front<double, kFma>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
-    e = cudaOccupancyMaxActiveClusters(&n, k_front<double, kFma>, &cfg);
+    cudaFuncSetAttribute(k_front<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
+    e = cudaOccupancyMaxActiveClusters(&n, k_front<double, false>, &cfg);
   } else {
-    cudaFuncSetAttribute(k_front<float, kFma>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
-    cudaFuncSetAttribute(k_front<float, kSplit>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
-    cudaFuncSetAttribute(k_front<float, kTf32>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
-    e = cudaOccupancyMaxActiveClusters(&n, k_front<float, kFma>, &cfg);
+    cudaFuncSetAttribute(k_front<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
+    cudaFuncSetAttribute(k_front<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
+    e = cudaOccupancyMaxActiveClusters(&n, k_front<float, false>, &cfg);
   }
   if (e != cudaSuccess) {
     cudaGetLastError();
