@@ -78,6 +78,11 @@ struct lsw_ctx {
   std::string dev_key;      // GPU identity for the tuner's cache (UUID, name, SM count)
   double tune_seconds = 0;  // time this context spent measuring front shapes
   int force_r = 0, force_cl = 0;   // one launch shape imposed on every front where it fits
+  // captured applies launch each front once per shifted decomposition on
+  // concurrent streams (side streams and fork/join events, created on first use)
+  bool split_shifts = true;
+  cudaStream_t side[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t side_ev[4] = {nullptr, nullptr, nullptr, nullptr};
   // bounded-wait limit of the sweep and factorisation kernels, in SM clock cycles
   long long wait_cycles = 4000000000LL;   // ~2 s at 2 GHz
   // device address of the allocation-free solve's fixed scratch array on this
@@ -107,6 +112,10 @@ struct lsw_ctx {
   ~lsw_ctx() {
     drop_graphs();
     if (cap_stream) cudaStreamDestroy(cap_stream);
+    for (auto& q : side)
+      if (q) cudaStreamDestroy(q);
+    for (auto& e : side_ev)
+      if (e) cudaEventDestroy(e);
   }
 };
 
@@ -243,7 +252,7 @@ lsw_status ensure_pools(lsw_ctx* ctx, int nrhs, long long scratch_elems) {
   return LSW_OK;
 }
 
-lsw_status launch_front_of(lsw_ctx* ctx, const Schedule* sc, size_t fi, cudaStream_t st);
+lsw_status launch_front_of(lsw_ctx* ctx, const Schedule* sc, size_t fi, cudaStream_t st, int i0 = 0, int i1 = -1);
 lsw_status check_kernel_err(lsw_ctx* ctx, cudaStream_t st);
 
 // ---- sweep-front autotuner ----
@@ -440,9 +449,9 @@ lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out, cudaStream_t st)
   return LSW_OK;
 }
 
-// One sweep front of schedule sc on stream st.  The input and output
-// addresses are read from ctx->d_ref.
-lsw_status launch_front_of(lsw_ctx* ctx, const Schedule* sc, size_t fi, cudaStream_t st) {
+// Items [i0, i1) (all for i1 < 0) of sweep front fi of schedule sc on stream
+// st.  The input and output addresses are read from ctx->d_ref.
+lsw_status launch_front_of(lsw_ctx* ctx, const Schedule* sc, size_t fi, cudaStream_t st, int i0, int i1) {
   FrontArgs a{};
   a.cells = ctx->d_cells.as<DevCell>();
   a.slots = sc->d_slots;
@@ -460,8 +469,10 @@ lsw_status launch_front_of(lsw_ctx* ctx, const Schedule* sc, size_t fi, cudaStre
   a.wait_cycles = ctx->wait_cycles;
   a.split = ctx->prec == LSW_PREC_SPLIT ? 1 : 0;
   const Front& f = sc->fronts[fi];
-  a.items = sc->d_items + f.item_begin;
-  a.item_count = f.item_count;
+  if (i1 < 0) i1 = f.item_count;
+  if (i1 <= i0) return LSW_OK;
+  a.items = sc->d_items + f.item_begin + i0;
+  a.item_count = i1 - i0;
   a.max_slots = f.max_slots;
   a.cluster = f.cluster;
   cudaError_t e = ctx->prec != LSW_PREC_C128 ? launch_front<float>(a, ctx->max_ny, ctx->max_nx, st)
@@ -475,17 +486,65 @@ lsw_status launch_front_of(lsw_ctx* ctx, const Schedule* sc, size_t fi, cudaStre
 // output addresses are read from ctx->d_ref (set by the caller beforehand),
 // so the sequence can be captured once and replayed for any vectors.
 // Returns the number of kernels enqueued in *kernels.
-lsw_status enqueue_apply(lsw_ctx* ctx, Schedule* sc, int nrhs, cudaStream_t st, int* kernels) {
+// With `split_shifts` (the captured applies), a front whose items each belong
+// to one shifted decomposition is launched once per shift, shift s on side
+// stream s (shift 0 on st): the four decompositions never share data before
+// their outputs are summed, so the launches of one shift's next front start
+// while other shifts still run, and the ends of the fronts overlap instead of
+// leaving SMs idle.  A mixed front joins every stream and runs alone.
+lsw_status enqueue_apply(lsw_ctx* ctx, Schedule* sc, int nrhs, cudaStream_t st, int* kernels,
+                         bool split_shifts = false) {
   const size_t cs = csize(ctx->prec);
   CK(cudaMemsetAsync(ctx->d_traces.p, 0, (size_t)nrhs * 4 * ctx->ncell * 24 * ctx->LP * cs, st), "memset traces");
   CK(cudaMemsetAsync(ctx->d_outs.p, 0, (size_t)nrhs * 4 * ctx->n2 * cs, st), "memset outs");
   int k = 0;
-  for (size_t fi = 0; fi < sc->fronts.size(); ++fi) {
-    if (ctx->front_events) CK(cudaEventRecord((*ctx->front_events)[2 * fi], st), "event");
-    lsw_status s = launch_front_of(ctx, sc, fi, st);
-    if (s != LSW_OK) return s;
-    if (ctx->front_events) CK(cudaEventRecord((*ctx->front_events)[2 * fi + 1], st), "event");
-    k += sc->fronts[fi].item_count > 0 ? 1 : 0;
+  if (split_shifts) {
+    for (int i = 0; i < 3; ++i)
+      if (!ctx->side[i]) CK(cudaStreamCreateWithFlags(&ctx->side[i], cudaStreamNonBlocking), "side stream");
+    for (int i = 0; i < 4; ++i)
+      if (!ctx->side_ev[i]) CK(cudaEventCreateWithFlags(&ctx->side_ev[i], cudaEventDisableTiming), "side event");
+    cudaStream_t ss[4] = {st, ctx->side[0], ctx->side[1], ctx->side[2]};
+    bool forked = false;
+    auto fork = [&]() -> lsw_status {
+      CK(cudaEventRecord(ctx->side_ev[0], st), "fork");
+      for (int i = 1; i < 4; ++i) CK(cudaStreamWaitEvent(ss[i], ctx->side_ev[0], 0), "fork wait");
+      forked = true;
+      return LSW_OK;
+    };
+    auto join = [&]() -> lsw_status {
+      for (int i = 1; i < 4; ++i) {
+        CK(cudaEventRecord(ctx->side_ev[i], ss[i]), "join");
+        CK(cudaStreamWaitEvent(st, ctx->side_ev[i], 0), "join wait");
+      }
+      forked = false;
+      return LSW_OK;
+    };
+    lsw_status s;
+    for (size_t fi = 0; fi < sc->fronts.size(); ++fi) {
+      const Front& f = sc->fronts[fi];
+      if (f.item_count <= 0) continue;
+      if (f.mixed) {
+        if (forked && (s = join()) != LSW_OK) return s;
+        if ((s = launch_front_of(ctx, sc, fi, st)) != LSW_OK) return s;
+        ++k;
+        continue;
+      }
+      if (!forked && (s = fork()) != LSW_OK) return s;
+      for (int sh = 0; sh < 4; ++sh) {
+        if (f.sh_begin[sh + 1] <= f.sh_begin[sh]) continue;
+        if ((s = launch_front_of(ctx, sc, fi, ss[sh], f.sh_begin[sh], f.sh_begin[sh + 1])) != LSW_OK) return s;
+        ++k;
+      }
+    }
+    if (forked && (s = join()) != LSW_OK) return s;
+  } else {
+    for (size_t fi = 0; fi < sc->fronts.size(); ++fi) {
+      if (ctx->front_events) CK(cudaEventRecord((*ctx->front_events)[2 * fi], st), "event");
+      lsw_status s = launch_front_of(ctx, sc, fi, st);
+      if (s != LSW_OK) return s;
+      if (ctx->front_events) CK(cudaEventRecord((*ctx->front_events)[2 * fi + 1], st), "event");
+      k += sc->fronts[fi].item_count > 0 ? 1 : 0;
+    }
   }
   double2* const* yref = reinterpret_cast<double2* const*>(ctx->d_ref.p) + 1;
   cudaError_t e = ctx->prec != LSW_PREC_C128 ? launch_combine_ref<float>(ctx->d_outs.p, yref, nrhs, ctx->n2, st)
@@ -512,7 +571,7 @@ lsw_status precond_impl(lsw_ctx* ctx, const double2* x, double2* y, int nrhs, cu
     if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
     if (!ctx->cap_stream) CK(cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking), "capture stream");
     CK(cudaStreamBeginCapture(ctx->cap_stream, cudaStreamCaptureModeRelaxed), "begin capture");
-    s = enqueue_apply(ctx, sc, nrhs, ctx->cap_stream, &kernels);
+    s = enqueue_apply(ctx, sc, nrhs, ctx->cap_stream, &kernels, ctx->split_shifts);
     cudaGraph_t graph = nullptr;
     const cudaError_t e = cudaStreamEndCapture(ctx->cap_stream, &graph);
     if (s != LSW_OK) {
@@ -673,6 +732,8 @@ lsw_status lsw_ctx_create(lsw_ctx** out, int device) {
   if (const char* ev = std::getenv("LSW_GRAPHS")) c->use_graphs = std::atoi(ev) != 0;
   // LSW_FACTOR_TC=1 runs the complex64 / split factorisation on the tensor cores
   if (const char* ev = std::getenv("LSW_FACTOR_TC")) c->factor_tc = std::atoi(ev) != 0;
+  // LSW_SHIFT_STREAMS=0 keeps each captured front one launch on one stream
+  if (const char* ev = std::getenv("LSW_SHIFT_STREAMS")) c->split_shifts = std::atoi(ev) != 0;
   // LSW_TUNE=0 leaves every sweep-front shape to the cost model
   if (const char* ev = std::getenv("LSW_TUNE")) c->tune = std::atoi(ev) != 0;
   // LSW_FRONT_SHAPE=RxC imposes R slots per item (4, 8, 16) and C CTAs per half

@@ -296,9 +296,12 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
   fronts.clear(); items.clear(); slots.clear(); groups.clear();
   for (size_t fidx = 0; fidx < fr.size(); ++fidx) {
     auto& f = fr[fidx];
+    // slots ordered by (shift, rhs): items of 8 or 16 slots merge the groups of
+    // one shifted decomposition when there are several right-hand sides, so
+    // that the front can run as one launch per shift (see below)
     for (auto& kv : f)
       std::stable_sort(kv.second.begin(), kv.second.end(), [](const SlotSpec& a, const SlotSpec& b) {
-        return std::make_tuple(a.rhs, a.shift, a.order) < std::make_tuple(b.rhs, b.shift, b.order);
+        return std::make_tuple(a.shift, a.rhs, a.order) < std::make_tuple(b.shift, b.rhs, b.order);
       });
     // choose the slots per item and the cluster size with the cost model
     int ny_max = 1, nx_max = 1;
@@ -376,14 +379,82 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
           it.group_count++;
         }
         it.slot_count = count;
-        it.scratch_off = F.scratch_elems;
-        F.scratch_elems += (long long)(cl.nx + 1) * front_rpad(it.slot_count) * cl.ny;
+        it.scratch_off = (long long)(cl.nx + 1) * front_rpad(it.slot_count) * cl.ny;   // its size, for now
         F.max_slots = std::max(F.max_slots, it.slot_count);
         items.push_back(it);
         F.item_count++;
       });
     }
+    // The four shifted decompositions never share data until their outputs
+    // are summed, so a front whose items each belong to one shift is run as
+    // one launch per shift (on concurrent streams, see enqueue_apply): its
+    // items are ordered by shift and sh_begin[s] .. sh_begin[s + 1] are those
+    // of shift s.  A front with an item that mixes shifts stays one launch.
+    {
+      auto item_shift = [&](const DevItem& it) {
+        int sh = groups[it.group_begin].shift;
+        for (int g = 1; g < it.group_count; ++g)
+          if (groups[it.group_begin + g].shift != sh) return -1;
+        return sh;
+      };
+      auto first = items.begin() + F.item_begin;
+      F.mixed = false;
+      for (auto it = first; it != items.end(); ++it)
+        if (item_shift(*it) < 0) F.mixed = true;
+      if (!F.mixed)
+        std::stable_sort(first, items.end(),
+                         [&](const DevItem& a, const DevItem& b) { return item_shift(a) < item_shift(b); });
+      for (int sh = 0; sh <= 4; ++sh) F.sh_begin[sh] = F.mixed ? (sh == 0 ? 0 : F.item_count) : 0;
+      if (!F.mixed) {
+        int cnt[4] = {0, 0, 0, 0};
+        for (auto it = first; it != items.end(); ++it) cnt[item_shift(*it)]++;
+        for (int sh = 0; sh < 4; ++sh) F.sh_begin[sh + 1] = F.sh_begin[sh] + cnt[sh];
+      }
+    }
     fronts.push_back(F);
+  }
+
+  // Scratch (each item's forward storage, sized above in scratch_off): the
+  // items of a front are live together; the launches of different shifts of
+  // consecutive fronts may run together, so each shift has its own region,
+  // sized for its largest front.  A mixed front runs alone (every shift's
+  // stream joined) and lays its items out from 0.  Every front records the
+  // pool size in scratch_elems.
+  long long region[4] = {0, 0, 0, 0}, mixed_max = 0;
+  for (const Front& F : fronts) {
+    if (F.mixed) {
+      long long t = 0;
+      for (int i = F.item_begin; i < F.item_begin + F.item_count; ++i) t += items[i].scratch_off;
+      mixed_max = std::max(mixed_max, t);
+      continue;
+    }
+    for (int sh = 0; sh < 4; ++sh) {
+      long long t = 0;
+      for (int i = F.item_begin + F.sh_begin[sh]; i < F.item_begin + F.sh_begin[sh + 1]; ++i) t += items[i].scratch_off;
+      region[sh] = std::max(region[sh], t);
+    }
+  }
+  const long long base[4] = {0, region[0], region[0] + region[1], region[0] + region[1] + region[2]};
+  const long long pool = std::max(base[3] + region[3], mixed_max);
+  for (Front& F : fronts) {
+    if (F.mixed) {
+      long long off = 0;
+      for (int i = F.item_begin; i < F.item_begin + F.item_count; ++i) {
+        const long long sz = items[i].scratch_off;
+        items[i].scratch_off = off;
+        off += sz;
+      }
+    } else {
+      for (int sh = 0; sh < 4; ++sh) {
+        long long off = base[sh];
+        for (int i = F.item_begin + F.sh_begin[sh]; i < F.item_begin + F.sh_begin[sh + 1]; ++i) {
+          const long long sz = items[i].scratch_off;
+          items[i].scratch_off = off;
+          off += sz;
+        }
+      }
+    }
+    F.scratch_elems = pool;
   }
 }
 

@@ -96,6 +96,8 @@ struct Front {
   int cluster;            // CTAs per item chosen for this front
   int slots_cap = 0;      // slots per item at most (the planner's r)
   float tuned_ms = -1.f;  // the tuner's timing of this shape, -1 when the cost model chose it
+  bool mixed = false;     // an item mixes shifted decompositions: the front is one launch
+  int sh_begin[5] = {0, 0, 0, 0, 0};   // items of shift s: [sh_begin[s], sh_begin[s + 1]) (not mixed)
 };
 
 // What the front planner knows about the device: how many clusters of each
