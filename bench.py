@@ -519,10 +519,16 @@ def run_serve(args):
         reqs = serving_stream(n_req, rate_hz=rate, seed=3 + i)
         st = eng.run(reqs, realtime=True)
         res = [r.true_rel_res for r in reqs if r.error is None]
+        errs = {}
+        for r in reqs:
+            if r.error is not None:
+                k = r.error[:160]
+                errs[k] = errs.get(k, 0) + 1
         print(json.dumps({"metric": "serving: p50/p99 latency and solves/s at rel. residual 1e-6",
                           "rate_hz": rate, "requests": len(reqs), "unit": "solves/s",
                           "value": st.solves_per_s, **st.as_dict(),
                           "max_true_rel_res": max(res) if res else None,
+                          "errors": errs,
                           "config": {"workload": "serving stream: grids {256,512,1024,2048}^2 of 128^2 cells, "
                                                  "6-10 ppw, lens/layered media with 30% repeats, 1-16 sources, "
                                                  "Poisson arrivals", "precision": "mixed", "slots": args.serve_slots,

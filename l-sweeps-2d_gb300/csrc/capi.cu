@@ -383,6 +383,8 @@ lsw_status tune_fronts(lsw_ctx* ctx, int nrhs, const FrontPlan& plan, cudaStream
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   CK(cudaStreamSynchronize(st), "tuning sync");
+  // the candidates' scratch may exceed the chosen schedule's: reallocated at its size
+  ctx->d_scratch.release();
   ctx->tune_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
   return s;
 }
