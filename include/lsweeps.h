@@ -156,8 +156,13 @@ const char* lsw_ctx_last_error(const lsw_ctx* ctx);
  * its kernels one by one (enable = 0).  One graph per batch size is captured
  * on first use and captured again when the context's sweep pools are
  * reallocated or released; both ways run the same kernels on the same data and
- * give identical results.  No counterpart in the reference (its applies are
- * host loops over MPI ranks, DDCheckerboard.cpp:687-739). */
+ * give identical results.  A capture can be invalidated by CUDA calls that
+ * other host threads make while it runs (allocations, frees, synchronous
+ * copies) and can make such calls fail: callers that drive the library from
+ * several threads at once turn graphs off.  A capture that fails is not an
+ * error: the context then launches every apply's kernels directly.  No
+ * counterpart in the reference (its applies are host loops over MPI ranks,
+ * DDCheckerboard.cpp:687-739). */
 lsw_status lsw_ctx_set_graphs(lsw_ctx* ctx, int enable);
 
 /* Sweep-front launch shapes.  Each front (one launch per stage step, every

@@ -100,6 +100,7 @@ struct lsw_ctx {
   };
   std::map<int, ApplyGraph> graphs;
   bool use_graphs = true;
+  int graph_failures = 0;   // captures that failed (the context then launches eagerly)
   long long pool_gen = 0;
   cudaStream_t cap_stream = nullptr;
   DevBuf d_ref;   // the captured applies' address table: input, output
@@ -576,15 +577,24 @@ lsw_status precond_impl(lsw_ctx* ctx, const double2* x, double2* y, int nrhs, cu
     s = enqueue_apply(ctx, sc, nrhs, ctx->cap_stream, &kernels, ctx->split_shifts);
     cudaGraph_t graph = nullptr;
     const cudaError_t e = cudaStreamEndCapture(ctx->cap_stream, &graph);
-    if (s != LSW_OK) {
-      if (graph) cudaGraphDestroy(graph);
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t ei = cudaErrorUnknown;
+    if (s == LSW_OK && e == cudaSuccess && graph) ei = cudaGraphInstantiate(&exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+      // A capture can be invalidated by CUDA calls of other host threads (an
+      // allocation or free, a synchronous copy) made while it runs.  The
+      // context stops capturing and this and later applies launch their
+      // kernels one by one, which give the same results.
+      if (exec) cudaGraphExecDestroy(exec);
+      cudaGetLastError();
+      ctx->use_graphs = false;
+      ctx->graph_failures += 1;
+      ctx->graphs.erase(nrhs);
+      s = enqueue_apply(ctx, sc, nrhs, st, &kernels);
+      ctx->launches += kernels;
       return s;
     }
-    CK(e, "end capture");
-    cudaGraphExec_t exec = nullptr;
-    const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    CK(ei, "graph instantiate");
     g.exec = exec;
     g.gen = ctx->pool_gen;
     g.kernels = kernels;

@@ -69,8 +69,8 @@ constexpr int kOffB = 3 * kATerm;
 constexpr int kOffF = kOffB + 3 * kBTerm;           // float2 [2][kB][kMaxRows]
 constexpr int kOffGU = kOffF + 2 * kB * kMaxRows * 8;              // float2 [kB][kMaxCols]
 constexpr int kOffU = kOffGU + kB * kMaxCols * 8;                  // float2 [kB][kMaxCols]
-constexpr int kOffRB = kOffU + kB * kMaxCols * 8;                  // float2 [2][kB + 1]
-constexpr int kOffInv = kOffRB + 2 * (kB + 1) * 8;                 // float2 [2][kB]
+constexpr int kOffRB = kOffU + kB * kMaxCols * 8;                  // float2 [2][8 warps][kB]
+constexpr int kOffInv = kOffRB + 2 * 8 * kB * 8;                   // float2 [2][kB]
 constexpr int kOffM1 = kOffInv + 2 * kB * 8;                       // float2 [kB][kB]
 constexpr int kOffInts = kOffM1 + kB * kB * 8;                     // used, piv, pslot, pinv [kMaxRows] each
 constexpr int kOffPb = kOffInts + 4 * kMaxRows * 4;                // int [2][kB]
@@ -81,6 +81,7 @@ constexpr int kSmem = kOffMisc + 16;
 static_assert(kOffF == 86016, "layout");
 static_assert(16 * kMaxRows * 8 <= 3 * kATerm, "unscramble staging tile [16][ldn] fits in the A operand area");
 static_assert(kOffBar % 8 == 0, "mbarrier alignment");
+static_assert(kMaxRows <= kT - 32, "the last warp holds no matrix row (it forms M1)");
 
 __device__ __forceinline__ unsigned saddr(const void* p) {
   return static_cast<unsigned>(__cvta_generic_to_shared(p));
@@ -126,14 +127,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity) {
       : "memory");
   return ok != 0;
 }
-// stores into CTA `rank`'s shared memory at the offset of p (ordered for the
-// peer by the cluster barrier that follows)
-__device__ __forceinline__ void st_remote(float2* p, unsigned rank, float2 v) {
-  asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(mapa(saddr(p), rank)), "f"(v.x), "f"(v.y)
-               : "memory");
+// loads from CTA `rank`'s shared memory at the offset of p (after a cluster
+// barrier that ordered the owner's writes)
+__device__ __forceinline__ float4 ld_remote4(const float4* p, unsigned rank) {
+  float4 v;
+  asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "r"(mapa(saddr(p), rank)));
+  return v;
 }
-__device__ __forceinline__ void st_remote(int* p, unsigned rank, int v) {
-  asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(mapa(saddr(p), rank)), "r"(v) : "memory");
+__device__ __forceinline__ float2 ld_remote(const float2* p, unsigned rank) {
+  float2 v;
+  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(mapa(saddr(p), rank)));
+  return v;
+}
+__device__ __forceinline__ int ld_remote(const int* p, unsigned rank) {
+  int v;
+  asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(mapa(saddr(p), rank)));
+  return v;
 }
 __device__ __forceinline__ void named_sync(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
@@ -258,7 +269,7 @@ k_factorize_tc(const DevCell* __restrict__ cells, const double2* __restrict__ pr
   C* F = reinterpret_cast<C*>(smem + kOffF);          // [2][kB][kMaxRows]
   C* GU = reinterpret_cast<C*>(smem + kOffGU);        // [kB][kMaxCols] pivot rows g, then their final values
   C* U = reinterpret_cast<C*>(smem + kOffU);          // [kB][kMaxCols] u = M1 g
-  C* RB = reinterpret_cast<C*>(smem + kOffRB);        // [2][kB + 1] scaled pivot row, 1/pivot last
+  C* RW = reinterpret_cast<C*>(smem + kOffRB);        // [2][8][kB] each warp's pivot candidate row
   C* invv = reinterpret_cast<C*>(smem + kOffInv);     // [2][kB]
   C* M1 = reinterpret_cast<C*>(smem + kOffM1);        // [kB][kB]
   int* used = reinterpret_cast<int*>(smem + kOffInts);
@@ -449,63 +460,59 @@ k_factorize_tc(const DevCell* __restrict__ cells, const double2* __restrict__ pr
 #pragma unroll
         for (int q = 0; q < kB; ++q) row[q] = (warp_rows && live && q < bt) ? make_float2(pv[2 * q], pv[2 * q + 1]) : z;
         bool mine_used = live ? (used[r] != 0) : true;
+        // One barrier per step: the candidate row of every warp (its largest
+        // unpivoted magnitude, found with one warp reduction) publishes its
+        // panel values before the barrier, and after it every thread reads
+        // the pivot row from its warp's slot and applies the step itself.
 #pragma unroll
         for (int t = 0; t < kB; ++t) {
           if (t >= bt) break;
           const int par = t & 1;
           const C v = row[t];
-          if (live) {
-            Fb_[(size_t)t * kMaxRows + r] = v;
-            for (int q = 0; q < G; ++q)
-              if (q != (int)g) st_remote(Fb_ + (size_t)t * kMaxRows + r, (unsigned)q, v);
-          }
+          if (live) Fb_[(size_t)t * kMaxRows + r] = v;
           // pivot key: |v|^2 as float bits (monotone for non-negative values) with
           // the low byte replaced by 255 - row: the largest magnitude, ties (to
           // 2^-15) to the lowest row; pivoted rows have key 0
           unsigned key = 0u;
           if (live && !mine_used) key = (__float_as_uint(abs2(v)) & 0xffffff00u) | (unsigned)(255 - r);
-          key = __reduce_max_sync(0xffffffffu, key);
+          const unsigned wmax = __reduce_max_sync(0xffffffffu, key);
+          C* rw = RW + (size_t)par * 8 * kB;
+          if (key != 0u && key == wmax) {
+            C* dst = rw + warp * kB;
+#pragma unroll
+            for (int q = 0; q < kB; ++q)
+              if (q < bt) dst[q] = row[q];
+          }
           unsigned* wk = wkey + par * 8;
-          if (lane == 0) wk[warp] = key;
+          if (lane == 0) wk[warp] = wmax;
           named_sync(1, kT);
           unsigned best = wk[0];
 #pragma unroll
           for (int w = 1; w < kT / 32; ++w) best = max(best, wk[w]);
           // best < 256: no unpivoted row of positive magnitude (singular); the
-          // step still runs on the lowest unpivoted row so that the kernel ends
-          // normally, and the status marks the factor invalid
+          // step still runs (on row 0, whatever its slot holds) so that the
+          // kernel ends normally, and the status marks the factor invalid
           if (best < 256u && r == 0) atomicOr(status, 1);
           const int p = best ? 255 - (int)(best & 0xffu) : 0;
-          C* rb = RB + par * (kB + 1);
+          const C* prow = rw + (p >> 5) * kB;
+          const C inv = crcp(prow[t]);
           if (r == p) {
             if (!isfinite(abs2(v))) atomicOr(status, 1);
-            const C inv = crcp(v);
             mine_used = true;
+#pragma unroll
+            for (int q = 0; q < kB; ++q)
+              if (q < bt) row[q] = (q == t) ? inv : cmul(row[q], inv);
             used[r] = 1;
             piv[k0 + t] = r;
             pbb[t] = r;
             ivb[t] = inv;
-            for (int q = 0; q < G; ++q)
-              if (q != (int)g) {
-                st_remote(pbb + t, (unsigned)q, r);
-                st_remote(ivb + t, (unsigned)q, inv);
-              }
+          } else if (live) {
+            const C vi = cmul(v, inv);
 #pragma unroll
             for (int q = 0; q < kB; ++q)
               if (q < bt) {
-                row[q] = (q == t) ? inv : cmul(row[q], inv);
-                rb[q] = row[q];
-              }
-            rb[kB] = inv;
-          }
-          named_sync(1, kT);
-          if (live && r != p) {
-            const C inv = rb[kB];
-#pragma unroll
-            for (int q = 0; q < kB; ++q)
-              if (q < bt) {
-                if (q == t) row[q] = cneg(cmul(v, inv));
-                else cfms(row[q], v, rb[q]);
+                if (q == t) row[q] = cneg(vi);
+                else cfms(row[q], vi, prow[q]);
               }
           }
         }
@@ -528,18 +535,40 @@ k_factorize_tc(const DevCell* __restrict__ cells, const double2* __restrict__ pr
         }
       }
       if (!csync()) { leave(); return; }
-      // the panel owner pushed f_t, the pivots and the reciprocals into every
-      // CTA's buffers before the cluster barrier
-      if ((int)g != o && tid < bt) {
-        const int p = pbb[tid];
-        used[p] = 1;
-        piv[k0 + tid] = p;
+      if ((int)g != o) {
+        // the panel owner's f_t, pivots and reciprocals, read from its shared
+        // memory: whole [bt][kMaxRows] planes as 16-byte loads, all of a
+        // thread's loads in flight before its stores
+        constexpr int kPer = (kB * kMaxRows / 2 + kT - 1) / kT;
+        const int nv4 = bt * kMaxRows / 2;
+        float4 buf4[kPer];
+        const float4* src4 = reinterpret_cast<const float4*>(Fb_);
+        float4* dst4 = reinterpret_cast<float4*>(Fb_);
+#pragma unroll
+        for (int i = 0; i < kPer; ++i) {
+          const int e = tid + i * kT;
+          if (e < nv4) buf4[i] = ld_remote4(src4 + e, (unsigned)o);
+        }
+#pragma unroll
+        for (int i = 0; i < kPer; ++i) {
+          const int e = tid + i * kT;
+          if (e < nv4) dst4[e] = buf4[i];
+        }
+        if (tid < bt) {
+          const int p = ld_remote(pbb + tid, (unsigned)o);
+          pbb[tid] = p;
+          ivb[tid] = ld_remote(ivb + tid, (unsigned)o);
+          used[p] = 1;
+          piv[k0 + tid] = p;
+        }
+        __syncthreads();
       }
       if (tid < bt) pslot[pbb[tid]] = tid;
       __syncthreads();
-      // M1 = (D + L)^-1 (D = diag f_t[p_t], L[t][s] = f_s[p_t], s < t), one warp,
+      // M1 = (D + L)^-1 (D = diag f_t[p_t], L[t][s] = f_s[p_t], s < t), by the
+      // last warp (no matrix row: free while the others write the A operand),
       // lane j solving for column j
-      if (warp == 0 && lane < bt) {
+      if (warp == kT / 32 - 1 && lane < bt) {
         C mm[kB];
 #pragma unroll
         for (int t = 0; t < kB; ++t) {
@@ -584,21 +613,34 @@ k_factorize_tc(const DevCell* __restrict__ cells, const double2* __restrict__ pr
       // u = M1 g per (pivot, column); the panel's own columns and pivots past
       // the block get u = 0
       const int pcol0 = (int)g == o ? k0 - c0 : nc, pcol1 = (int)g == o ? k1 - c0 : nc;
-      for (int e = tid; e < kB * nc; e += kT) {
-        const int t = e / nc, cc = e - t * nc;
-        C a = z;
-        if (t < bt && (cc < pcol0 || cc >= pcol1))
-          for (int s2 = 0; s2 <= t; ++s2) cfma(a, M1[t * kB + s2], GU[(size_t)s2 * kMaxCols + cc]);
-        U[(size_t)t * kMaxCols + cc] = a;
+      {
+        int t = tid / nc, cc = tid - (tid / nc) * nc;   // element e = t nc + cc, advanced by kT
+        const int st_t = kT / nc, st_c = kT - (kT / nc) * nc;
+        for (int e = tid; e < kB * nc; e += kT) {
+          C a = z;
+          if (t < bt && (cc < pcol0 || cc >= pcol1))
+            for (int s2 = 0; s2 <= t; ++s2) cfma(a, M1[t * kB + s2], GU[(size_t)s2 * kMaxCols + cc]);
+          U[(size_t)t * kMaxCols + cc] = a;
+          t += st_t;
+          cc += st_c;
+          if (cc >= nc) { cc -= nc; ++t; }
+        }
       }
       __syncthreads();
       // B operand rows 2c: (Re u, -Im u), 2c + 1: (Im u, Re u) along k = (2t,
       // 2t + 1); the padding columns get zeros
-      for (int e = tid; e < kB * (NP / 2); e += kT) {
-        const int t = e / (NP / 2), cc = e - t * (NP / 2);
-        const C u = cc < nc ? U[(size_t)t * kMaxCols + cc] : z;
-        put3(Bop, kBTerm, kmaj(2 * cc, 2 * t), u.x, -u.y);
-        put3(Bop, kBTerm, kmaj(2 * cc + 1, 2 * t), u.y, u.x);
+      {
+        const int nh = NP / 2;
+        int t = tid / nh, cc = tid - (tid / nh) * nh;
+        const int st_t = kT / nh, st_c = kT - (kT / nh) * nh;
+        for (int e = tid; e < kB * nh; e += kT) {
+          const C u = cc < nc ? U[(size_t)t * kMaxCols + cc] : z;
+          put3(Bop, kBTerm, kmaj(2 * cc, 2 * t), u.x, -u.y);
+          put3(Bop, kBTerm, kmaj(2 * cc + 1, 2 * t), u.y, u.x);
+          t += st_t;
+          cc += st_c;
+          if (cc >= nh) { cc -= nh; ++t; }
+        }
       }
       // operand writes (generic proxy) visible to the tensor core (async proxy)
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -631,12 +673,19 @@ k_factorize_tc(const DevCell* __restrict__ cells, const double2* __restrict__ pr
       // while the tensor cores run: the block's pivot rows, which the product
       // leaves as they were, c[p_t] = u_t - sum_{s>t} f_s[p_t] u_s on my columns
       // outside the panel, into GU
-      for (int e = tid; e < bt * nc; e += kT) {
-        const int t = e / nc, cc = e - t * nc;
-        C a = U[(size_t)t * kMaxCols + cc];
-        const int pt = pbb[t];
-        for (int s2 = t + 1; s2 < bt; ++s2) cfms(a, Fb_[(size_t)s2 * kMaxRows + pt], U[(size_t)s2 * kMaxCols + cc]);
-        GU[(size_t)t * kMaxCols + cc] = a;
+      {
+        int t = tid / nc, cc = tid - (tid / nc) * nc;
+        const int st_t = kT / nc, st_c = kT - (kT / nc) * nc;
+        for (int e = tid; e < bt * nc; e += kT) {
+          C a = U[(size_t)t * kMaxCols + cc];
+          const int pt = pbb[t];
+          for (int s2 = t + 1; s2 < bt; ++s2)
+            cfms(a, Fb_[(size_t)s2 * kMaxRows + pt], U[(size_t)s2 * kMaxCols + cc]);
+          GU[(size_t)t * kMaxCols + cc] = a;
+          t += st_t;
+          cc += st_c;
+          if (cc >= nc) { cc -= nc; ++t; }
+        }
       }
       __syncthreads();
       if (!wait_mma(true)) { leave(); return; }

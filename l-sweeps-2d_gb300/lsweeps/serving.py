@@ -147,6 +147,12 @@ class GpuOperator:
     def __init__(self, spec: ProblemSpec, m_grid: np.ndarray, precision: str, device: int, stream):
         from .solver import Solver
         self.solver = Solver(spec, m_grid, precision=precision, device=device)
+        # several slots run operators from their own host threads: a CUDA-graph
+        # capture in one thread can be invalidated by another thread's
+        # allocations, frees or synchronous copies (and invalidate their
+        # calls), so serving launches every apply's kernels directly (launch
+        # overhead is < 1 % of an apply)
+        self.solver.set_graphs(False)
         try:
             self.solver.factorize(stream=stream)
         except BaseException:

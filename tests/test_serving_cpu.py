@@ -271,6 +271,9 @@ def test_gpu_operator_closes_its_solver_when_factorisation_fails(monkeypatch):
         def __init__(self, *a, **k):
             events.append("init")
 
+        def set_graphs(self, enable):
+            events.append(f"graphs {int(enable)}")
+
         def factorize(self, stream=None):
             raise RuntimeError("LSW_ERR_OUT_OF_MEMORY: cudaMalloc(factors): out of memory")
 
@@ -280,4 +283,5 @@ def test_gpu_operator_closes_its_solver_when_factorisation_fails(monkeypatch):
     monkeypatch.setattr(solver_mod, "Solver", FakeSolver)
     with pytest.raises(RuntimeError):
         GpuOperator(_spec(), np.ones((1, 1)), "c64", 0, None)
-    assert events == ["init", "close"]
+    # serving operators launch directly (no graph capture across slots)
+    assert events == ["init", "graphs 0", "close"]
