@@ -72,7 +72,7 @@ struct lsw_ctx {
   int krylov_batch = 0;   // right-hand sides per Krylov sub-batch at most (0: as memory allows)
   bool factor_lookahead = true;
   // complex64 / split factorisation on the tensor cores (else the CUDA-core kernel)
-  bool factor_tc = false;
+  bool factor_tc = true;
   // sweep-front shapes measured on the device on first use (else the cost model)
   bool tune = true;
   std::string dev_key;      // GPU identity for the tuner's cache (UUID, name, SM count)
@@ -742,7 +742,7 @@ lsw_status lsw_ctx_create(lsw_ctx** out, int device) {
   if (const char* ev = std::getenv("LSW_FACTOR_LOOKAHEAD")) c->factor_lookahead = std::atoi(ev) != 0;
   // LSW_GRAPHS=0 launches every apply's kernels one by one instead of replaying a CUDA graph
   if (const char* ev = std::getenv("LSW_GRAPHS")) c->use_graphs = std::atoi(ev) != 0;
-  // LSW_FACTOR_TC=1 runs the complex64 / split factorisation on the tensor cores
+  // LSW_FACTOR_TC=0 runs the complex64 / split factorisation on the CUDA cores
   if (const char* ev = std::getenv("LSW_FACTOR_TC")) c->factor_tc = std::atoi(ev) != 0;
   // LSW_SHIFT_STREAMS=0 keeps each captured front one launch on one stream
   if (const char* ev = std::getenv("LSW_SHIFT_STREAMS")) c->split_shifts = std::atoi(ev) != 0;

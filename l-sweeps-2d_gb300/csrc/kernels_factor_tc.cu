@@ -271,7 +271,7 @@ k_factorize_tc(const DevCell* __restrict__ cells, const double2* __restrict__ pr
   C* U = reinterpret_cast<C*>(smem + kOffU);          // [kB][kMaxCols] u = M1 g
   C* RW = reinterpret_cast<C*>(smem + kOffRB);        // [2][8][kB] each warp's pivot candidate row
   C* invv = reinterpret_cast<C*>(smem + kOffInv);     // [2][kB]
-  C* M1 = reinterpret_cast<C*>(smem + kOffM1);        // [kB][kB]
+  C* M1 = reinterpret_cast<C*>(smem + kOffM1);        // [kB][kB], transposed: M1[s][t] at s kB + t
   int* used = reinterpret_cast<int*>(smem + kOffInts);
   int* piv = used + kMaxRows;
   int* pslot = piv + kMaxRows;
@@ -578,12 +578,13 @@ k_factorize_tc(const DevCell* __restrict__ cells, const double2* __restrict__ pr
             for (int s2 = 0; s2 < kB; ++s2)
               if (s2 < t) cfms(a, Fb_[(size_t)s2 * kMaxRows + pbb[t]], mm[s2]);
             mm[t] = cmul(a, ivb[t]);
-            M1[t * kB + lane] = mm[t];
+            M1[lane * kB + t] = mm[t];   // stored transposed: [s][t]
           }
         }
       }
-      // A operand: f_t[r] as (Re, Im) along k, three bf16 terms; zero rows for
-      // the block's pivot rows (finished on the CUDA cores after the product)
+      // A operand: f_t[r] as (Re, Im) along k, three bf16 terms, one row per
+      // thread; zero rows for the block's pivot rows (finished on the CUDA
+      // cores after the product) and past the matrix
       if (r < 128 * ntiles) {
         const bool is_piv = live && pslot[r] >= 0;
 #pragma unroll
@@ -610,36 +611,23 @@ k_factorize_tc(const DevCell* __restrict__ cells, const double2* __restrict__ pr
         }
       }
       __syncthreads();
-      // u = M1 g per (pivot, column); the panel's own columns and pivots past
-      // the block get u = 0
+      // u = M1 g per (pivot, column), into U and as the B operand: rows 2c:
+      // (Re u, -Im u), 2c + 1: (Im u, Re u) along k = (2t, 2t + 1).  The panel's
+      // own columns, pivots past the block and the padding columns get u = 0.
+      // A warp covers two units of 4 columns x 4 pivots (lane: column mod 4 =
+      // (lane >> 2) mod 4, pivot mod 4 = lane mod 4): two lanes per bank.
       const int pcol0 = (int)g == o ? k0 - c0 : nc, pcol1 = (int)g == o ? k1 - c0 : nc;
       {
-        int t = tid / nc, cc = tid - (tid / nc) * nc;   // element e = t nc + cc, advanced by kT
-        const int st_t = kT / nc, st_c = kT - (kT / nc) * nc;
-        for (int e = tid; e < kB * nc; e += kT) {
+        const int nh = NP / 2;   // columns with padding, a multiple of 8
+        for (int u2 = warp; u2 < nh / 2; u2 += kT / 32) {
+          const int u = u2 * 2 + (lane >> 4);   // unit: (column quarter-block, pivot quarter)
+          const int cc = (u >> 2) * 4 + ((lane >> 2) & 3), t = (u & 3) * 4 + (lane & 3);
           C a = z;
-          if (t < bt && (cc < pcol0 || cc >= pcol1))
-            for (int s2 = 0; s2 <= t; ++s2) cfma(a, M1[t * kB + s2], GU[(size_t)s2 * kMaxCols + cc]);
-          U[(size_t)t * kMaxCols + cc] = a;
-          t += st_t;
-          cc += st_c;
-          if (cc >= nc) { cc -= nc; ++t; }
-        }
-      }
-      __syncthreads();
-      // B operand rows 2c: (Re u, -Im u), 2c + 1: (Im u, Re u) along k = (2t,
-      // 2t + 1); the padding columns get zeros
-      {
-        const int nh = NP / 2;
-        int t = tid / nh, cc = tid - (tid / nh) * nh;
-        const int st_t = kT / nh, st_c = kT - (kT / nh) * nh;
-        for (int e = tid; e < kB * nh; e += kT) {
-          const C u = cc < nc ? U[(size_t)t * kMaxCols + cc] : z;
-          put3(Bop, kBTerm, kmaj(2 * cc, 2 * t), u.x, -u.y);
-          put3(Bop, kBTerm, kmaj(2 * cc + 1, 2 * t), u.y, u.x);
-          t += st_t;
-          cc += st_c;
-          if (cc >= nh) { cc -= nh; ++t; }
+          if (t < bt && cc < nc && (cc < pcol0 || cc >= pcol1))
+            for (int s2 = 0; s2 <= t; ++s2) cfma(a, M1[s2 * kB + t], GU[(size_t)s2 * kMaxCols + cc]);
+          if (cc < nc) U[(size_t)t * kMaxCols + cc] = a;
+          put3(Bop, kBTerm, kmaj(2 * cc, 2 * t), a.x, -a.y);
+          put3(Bop, kBTerm, kmaj(2 * cc + 1, 2 * t), a.y, a.x);
         }
       }
       // operand writes (generic proxy) visible to the tensor core (async proxy)
@@ -649,8 +637,10 @@ k_factorize_tc(const DevCell* __restrict__ cells, const double2* __restrict__ pr
       tc_fence_after();
       // ---- the block's update on the tensor cores: W -= F U, bf16 x 3 ----
       // (A term i, B term j) for i + j <= 2: hi hi, hi mid, mid hi, hi lo,
-      // mid mid, lo hi; two k-steps of 16 per 128-row tile
-      if (tid == 0) {
+      // mid mid, lo hi; two k-steps of 16 per 128-row tile.  Issued by the last
+      // warp (no matrix row), while the others form the pivot rows' values.
+      const int issuer = kT - 32;
+      if (tid == issuer) {
         const unsigned a0 = saddr(Aop), b0 = saddr(Bop);
         for (int tile = 0; tile < ntiles; ++tile) {
           const unsigned d = tbase + (unsigned)(256 * tile);
@@ -673,10 +663,10 @@ k_factorize_tc(const DevCell* __restrict__ cells, const double2* __restrict__ pr
       // while the tensor cores run: the block's pivot rows, which the product
       // leaves as they were, c[p_t] = u_t - sum_{s>t} f_s[p_t] u_s on my columns
       // outside the panel, into GU
-      {
+      if (tid < issuer) {
         int t = tid / nc, cc = tid - (tid / nc) * nc;
-        const int st_t = kT / nc, st_c = kT - (kT / nc) * nc;
-        for (int e = tid; e < bt * nc; e += kT) {
+        const int st_t = issuer / nc, st_c = issuer - (issuer / nc) * nc;
+        for (int e = tid; e < bt * nc; e += issuer) {
           C a = U[(size_t)t * kMaxCols + cc];
           const int pt = pbb[t];
           for (int s2 = t + 1; s2 < bt; ++s2)

@@ -44,17 +44,26 @@ def c2():
         yield spec, med, Q
 
 
-def test_c2_precond_matches_oracle(c2):
+def test_c2_precond_matches_oracle(c2, monkeypatch):
+    """M^-1 v at C2 against the oracle.  The complex64 and split factors carry
+    FP32 rounding, which the Schur recurrences of C2's 163-165-DOF cells
+    amplify to ~2e-4 with the block updates on the CUDA cores (FMAs, rounded to
+    nearest) and to ~3.4e-4 with the block updates on the tensor cores (their
+    FP32 accumulation into TMEM rounds differently); both give the FP64 solve's
+    iteration count and solution (test_mixed_precision_matches_fp64_at_scale)."""
     spec, med, Q = c2
     rng = np.random.default_rng(2)
     n2 = Q.n_dof ** 2
     v = rng.standard_normal(n2) + 1j * rng.standard_normal(n2)
     y_or = Q.apply_precond_global(v)
-    for prec, tol in (("c128", 1e-10), ("c64", 2e-4), ("bf16x2", 2e-4)):
+    cases = (("c128", "1", 1e-10), ("c64", "0", 2e-4), ("c64", "1", 5e-4), ("bf16x2", "0", 2e-4),
+             ("bf16x2", "1", 5e-4))
+    for prec, tc, tol in cases:
+        monkeypatch.setenv("LSW_FACTOR_TC", tc)
         S = _solver(spec, med, prec)
         y = S.apply_precond(torch.from_numpy(v).cuda()).cpu().numpy()
         S.close()
-        assert rel(y, y_or) <= tol, prec
+        assert rel(y, y_or) <= tol, (prec, tc, rel(y, y_or))
 
 
 def test_c2_reference_gmres_matches_oracle(c2):
