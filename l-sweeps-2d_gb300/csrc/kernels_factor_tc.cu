@@ -15,9 +15,11 @@
 //     tcgen05.st.
 //   * The panel (the B columns of a block, on the CTA that owns them) runs the
 //     classic Gauss-Jordan steps with each row's panel part in its thread's
-//     registers; per step one named barrier publishes the warps' pivot keys
-//     and a second one the scaled pivot row (double-buffered by step parity).
-//     It records f_t (column t at step t), the pivots p_t and 1 / f_t[p_t].
+//     registers, one CTA barrier per step: each warp's candidate row (its
+//     largest unpivoted magnitude, one warp reduction) writes its panel values
+//     and the warp's key before the barrier (double-buffered by step parity);
+//     after it every thread reads the pivot row and applies the step.  It
+//     records f_t (column t at step t), the pivots p_t and 1 / f_t[p_t].
 //   * Every other column then receives the B steps at once.  With
 //     u = M1 g (g the pivot rows, M1 = (D + L)^-1 of the pivots' f values)
 //     the rank-B update of the rows that are not pivots of the block is one
@@ -38,9 +40,10 @@
 //   * Unscrambled column-major into the factor pool through a shared-memory
 //     staging tile (Sinv[i][j] = W[piv[i]][pinv[j]]).
 // A thread-block cluster of G CTAs (G = 2 for cells of 97-192 DOFs per side)
-// splits the columns; the CTA owning a panel publishes f_t, p_t and 1/f_t[p_t]
-// through distributed shared memory, and the cluster meets once per block on
-// an mbarrier.  Every wait is bounded (a wait that runs out sets bit 1 of
+// splits the columns; after the cluster barrier that follows a panel the
+// other CTAs read its f_t, p_t and 1/f_t[p_t] from the owner's shared memory
+// (distributed shared memory), and the cluster meets once per block on an
+// mbarrier.  Every wait is bounded (a wait that runs out sets bit 1 of
 // *status, later waits return at once, TMEM is released and the CTA leaves
 // after the cluster's exit rendezvous).  A zero or non-finite pivot sets bit 0.
 #include "common.cuh"
