@@ -329,7 +329,12 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   const int nJ = je - jb;               // my columns / rows of every line
   const int RG = (ny + 63) >> 6;        // row groups of 64 rows
   // consumer warps: KSW column slices per row group, or (split) one per 16-row m-tile
-  const int NCW = SPLIT ? (ny + 15) >> 4 : KSW * RG;
+  // FP32/FP64 FMA matvec: KSW column slices per row group; with more than 8
+  // slots (complex64) two slot groups of R / 2 slots each, on their own warps,
+  // so that a warp keeps at most 8 slots of two rows in registers
+  constexpr int SG = (!SPLIT && sizeof(T) == 4 && R > 8) ? 2 : 1;
+  constexpr int RS = R / SG;
+  const int NCW = SPLIT ? (ny + 15) >> 4 : KSW * RG * SG;
   constexpr int NT = (2 * R + 7) / 8;   // split: n-tiles of 8 (Re, Im interleaved per slot)
   constexpr int NT8 = NT * 8;
   const int NCT = NCW * 32;
@@ -643,7 +648,8 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   const int cw = warp - kAux;
   if (cw >= NCW) return;   // idle warp (small cell)
   const int ct = cw * 32 + lane;
-  const int rg = cw / KSW, ks = cw % KSW;
+  const int sg = cw / (KSW * RG), rg = (cw / KSW) % RG, ks = cw % KSW;   // FMA matvec: slot group, row group, slice
+  const int sb = sg * RS;                                                  // first slot of my slot group
   const int r0 = rg * 64 + 2 * lane;    // my row pair
   const bool rows_ok = r0 < ldn;
 
@@ -738,9 +744,9 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
       }
     } else {
       // ---- partial products of my row pair with my slice of my columns ----
-      C acc0[R], acc1[R];
+      C acc0[RS], acc1[RS];
   #pragma unroll
-      for (int r = 0; r < R; ++r) { acc0[r] = czero<C>(); acc1[r] = czero<C>(); }
+      for (int r = 0; r < RS; ++r) { acc0[r] = czero<C>(); acc1[r] = czero<C>(); }
       for (int c = 0; c < nch; ++c, ++idx) {
         const int slot = (int)(idx % NS);
         const bool ok = mbar_wait<false>(&full[slot], (unsigned)((idx / NS) & 1), a.err, abort_flag, a.wait_cycles);
@@ -749,14 +755,14 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
         const int ncol = min(CW, nJ - c0);
         if (ok && rows_ok) {
           // deeper unrolling (more loads in flight) where the registers allow
-          constexpr int UNR = (R <= 4 && sizeof(T) == 4) ? 4 : 2;
+          constexpr int UNR = (RS <= 4 && sizeof(T) == 4) ? 4 : 2;
   #pragma unroll UNR
           for (int cc = ks; cc < ncol; cc += KSW) {
             Pair<T> s;
             s.load(S + (size_t)cc * ldn);
-            const C* v = V + (size_t)(c0 + cc) * R;
+            const C* v = V + (size_t)(c0 + cc) * R + sb;
   #pragma unroll
-            for (int r = 0; r < R; ++r) {
+            for (int r = 0; r < RS; ++r) {
               const C vr = v[r];
               cfma(acc0[r], s.a, vr);
               cfma(acc1[r], s.b, vr);
@@ -772,16 +778,16 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
       // float, and consecutive lanes hit consecutive banks)
       const int RG64 = 64 * RG;
       {
-        C* ls = LS + (size_t)ks * R * RG64 + r0;
+        C* ls = LS + ((size_t)ks * R + sb) * RG64 + r0;
   #pragma unroll
-        for (int r = 0; r < R; ++r) { ls[(size_t)r * RG64] = acc0[r]; ls[(size_t)r * RG64 + 1] = acc1[r]; }
+        for (int r = 0; r < RS; ++r) { ls[(size_t)r * RG64] = acc0[r]; ls[(size_t)r * RG64 + 1] = acc1[r]; }
       }
-      named_sync(3 + rg, KSW * 32);
+      named_sync(3 + rg, KSW * SG * 32);
       {
         constexpr int UP = (sizeof(T) == 4 && R % 2 == 0) ? 2 : 1;   // slots per store
         constexpr int NU = R / UP;                                  // stores per row
         const size_t lsplane = (size_t)R * RG64;
-        for (int u = ks * 32 + lane; u < 64 * NU; u += KSW * 32) {
+        for (int u = (sg * KSW + ks) * 32 + lane; u < 64 * NU; u += KSW * SG * 32) {
           const int up = u >> 6, rr = u & 63;   // consecutive lanes take consecutive rows
           const int row = rg * 64 + rr;
           if (row >= ny) continue;
@@ -938,7 +944,11 @@ bool front_shape(int max_ny, int max_nx, int R, int CL, bool split, int maxopt, 
   // column slices: as many as keep >= 4 columns per slice and the slices'
   // partial-sum staging (KSW x 192 x R) within 64 KB
   int KSW = kMaxKSW;
-  while (KSW > 1 && (split || nJmax < 4 * KSW || (size_t)KSW * 64 * kMaxRG * R * sizeof(cx_t<T>) > 65536)) --KSW;
+  // (complex64 with more than 8 slots: two slot groups, so at most 2 slices)
+  const int sgroups = (!split && sizeof(T) == 4 && R > 8) ? 2 : 1;
+  while (KSW > 1 && (split || nJmax < 4 * KSW || KSW * sgroups > kMaxKSW ||
+                     (size_t)KSW * 64 * kMaxRG * R * sizeof(cx_t<T>) > 65536))
+    --KSW;
   const int cwmax = (int)std::min<size_t>(((size_t)65536 / ((size_t)ldn * sizeof(cx_t<T>))) & ~size_t(7),
                                           (size_t)((nJmax + 7) & ~7));
   int CW = std::max(8, cwmax), NS = 0;
