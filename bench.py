@@ -489,12 +489,29 @@ def run_apply_only(args):
     prec = args.precision or PRECISION[args.config.upper()]
     S = Solver(spec, med, precision=prec)
     S.factorize()
+    shapes, tune_s = S.front_shapes(args.nrhs)   # tuned before anything is timed
     v = torch.randn(S.n2 * args.nrhs, dtype=torch.complex128, device="cuda")
-    for _ in range(args.warmup + args.steps):
-        S.apply_precond(v)
-    torch.cuda.synchronize()
+    y = torch.empty_like(v)
+    for _ in range(args.warmup):
+        S.apply_precond(v, out=y)
+    st = torch.cuda.current_stream()
+    ts = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        S.apply_precond(v, out=y)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
     line = {"apply_only": args.config, "precision": prec, "nrhs": args.nrhs,
-            "applies": args.warmup + args.steps, "fronts_per_apply": 3 * spec.N - 3 + 1}
+            "applies": args.warmup + args.steps, "fronts_per_apply": 3 * spec.N - 3 + 1,
+            "tune_s": round(tune_s, 2),
+            "shapes": " ".join("%dx%d%s" % (f["slots_cap"], f["cluster"], "t" if f["tensor_cores"] else "")
+                               for f in shapes)}
+    if ts:
+        # graph-replayed applies, CUDA events on the launching stream
+        med_ms = statistics.median(ts)
+        line.update({"apply_ms": round(med_ms, 3), "apply_ms_per_rhs": round(med_ms / args.nrhs, 3)})
     if args.warmup + args.steps > 0:
         # the algorithmic and streamed bytes of one apply (one more, profiled, apply)
         _, pr = S.apply_precond_profiled(v)

@@ -187,6 +187,7 @@ typedef struct {
   int slots_cap;    /* slots per item at most */
   int cluster;      /* CTAs per half chain */
   float tuned_ms;   /* the tuner's time for this front's shape; -1 when the cost model chose it */
+  int tensor_cores; /* 1: the line products run on the tensor cores (complex64, tcgen05) */
 } lsw_front_shape;
 
 /* The launch shapes of the sweep fronts of a batch of nrhs right-hand sides

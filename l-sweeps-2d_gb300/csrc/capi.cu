@@ -78,6 +78,12 @@ struct lsw_ctx {
   std::string dev_key;      // GPU identity for the tuner's cache (UUID, name, SM count)
   double tune_seconds = 0;  // time this context spent measuring front shapes
   int force_r = 0, force_cl = 0;   // one launch shape imposed on every front where it fits
+  bool force_tc = false;           // ... with its line products on the tensor cores (complex64)
+  // complex64: the tuner also measures each front with its line products on
+  // the tensor cores (tcgen05, items of 8 or 16 slots); off by default: on
+  // GB300 those launches were slower than the FMA matvec at every measured
+  // shape and less accurate (FP32 accumulation in the tensor core over long k)
+  bool sweep_tc = false;
   // captured applies launch each front once per shifted decomposition on
   // concurrent streams (side streams and fork/join events, created on first use)
   bool split_shifts = true;
@@ -224,6 +230,7 @@ FrontPlan base_plan(const lsw_ctx* ctx) {
   for (int r = 1; r <= 16; ++r)
     plan.fit_mask[r] = front_fit_mask(dbl, ctx->prec == LSW_PREC_SPLIT, ctx->max_ny, ctx->max_nx, r);
   if (plan.max_clusters[1] <= 0) plan.max_clusters[1] = ctx->nsm / 2;
+  plan.tc_scratch = ctx->prec == LSW_PREC_C64 && (ctx->sweep_tc || ctx->force_tc);
   return plan;
 }
 
@@ -258,7 +265,8 @@ lsw_status check_kernel_err(lsw_ctx* ctx, cudaStream_t st);
 
 // ---- sweep-front autotuner ----
 // On the first apply of a batch size the shape of every front -- slots per
-// item (4, 8, 16) and CTAs per half chain (1, 2, 4) -- is measured on the
+// item (4, 8, 16), CTAs per half chain (1, 2, 4) and, for complex64, line
+// products on the CUDA cores or the tensor cores -- is measured on the
 // device: each candidate shape is imposed on every front it fits, each front
 // whose launch is new is run twice and timed the second time with CUDA events
 // (the kernels' work does not depend on the values, so a zero vector serves),
@@ -266,17 +274,25 @@ lsw_status check_kernel_err(lsw_ctx* ctx, cudaStream_t st);
 // problem shape (precision, cells, cell size, PML, batch size) for the
 // process, and in the file named by LSW_TUNE_CACHE when it is set.
 struct TuneEntry {
-  std::vector<int> r, cl;
+  std::vector<int> r, cl, tc;
   std::vector<float> ms;
 };
+
+// whether the tuner measures tensor-core line products, and whether a front
+// of `max_slots` slots per item on clusters of 2 cl CTAs can run them
+bool tc_candidates(const lsw_ctx* ctx) { return ctx->prec == LSW_PREC_C64 && ctx->sweep_tc; }
+bool tc_fits(const lsw_ctx* ctx, int max_slots, int cl) {
+  if (ctx->prec != LSW_PREC_C64 || max_slots < 1 || max_slots > 16) return false;
+  return (front_fit_mask(false, false, ctx->max_ny, ctx->max_nx, front_tc_slots(max_slots), true) >> cl) & 1;
+}
 std::mutex g_tune_mu;
 std::map<std::string, TuneEntry> g_tune_cache;
 bool g_tune_file_read = false;
 
 std::string tune_key(const lsw_ctx* ctx, int nrhs) {
   char b[160];
-  std::snprintf(b, sizeof(b), "|prec%d|N%d|m%d|p%d|rhs%d|cl%d", ctx->prec, ctx->N, ctx->m, ctx->p, nrhs,
-                ctx->max_cluster);
+  std::snprintf(b, sizeof(b), "|prec%d|N%d|m%d|p%d|rhs%d|cl%d|tc%d", ctx->prec, ctx->N, ctx->m, ctx->p, nrhs,
+                ctx->max_cluster, (int)tc_candidates(ctx));
   return ctx->dev_key + b;
 }
 
@@ -298,7 +314,8 @@ void tune_file_read() {
       int r = 0, cl = 0;
       float ms = -1.f;
       if (std::sscanf(tok, "%d,%d,%f", &r, &cl, &ms) != 3) { e.r.clear(); break; }
-      e.r.push_back(r); e.cl.push_back(cl); e.ms.push_back(ms);
+      // slots per item, + 100 for tensor-core line products
+      e.r.push_back(r % 100); e.cl.push_back(cl); e.ms.push_back(ms); e.tc.push_back(r >= 100 ? 1 : 0);
     }
     if (!e.r.empty()) g_tune_cache[key] = e;
   }
@@ -311,7 +328,8 @@ void tune_file_append(const std::string& key, const TuneEntry& e) {
   FILE* f = std::fopen(path, "a");
   if (!f) return;
   std::fprintf(f, "%s", key.c_str());
-  for (size_t i = 0; i < e.r.size(); ++i) std::fprintf(f, " %d,%d,%.9g", e.r[i], e.cl[i], e.ms[i]);
+  for (size_t i = 0; i < e.r.size(); ++i)
+    std::fprintf(f, " %d,%d,%.9g", e.r[i] + (i < e.tc.size() && e.tc[i] ? 100 : 0), e.cl[i], e.ms[i]);
   std::fprintf(f, "\n");
   std::fclose(f);
 }
@@ -326,7 +344,8 @@ lsw_status tune_fronts(lsw_ctx* ctx, int nrhs, const FrontPlan& plan, cudaStream
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   CK(cudaEventCreate(&e0), "cudaEventCreate");
   CK(cudaEventCreate(&e1), "cudaEventCreate");
-  std::vector<std::map<std::tuple<int, int, int>, float>> seen;   // per front: (items, max slots, cluster) -> ms
+  // per front: (items, max slots, cluster, tensor cores) -> ms
+  std::vector<std::map<std::tuple<int, int, int, int>, float>> seen;
   lsw_status s = LSW_OK;
   for (int r : {4, 8, 16}) {
     if (r > plan.rmax) continue;
@@ -347,36 +366,41 @@ lsw_status tune_fronts(lsw_ctx* ctx, int nrhs, const FrontPlan& plan, cudaStream
       if (out->r.empty()) {
         out->r.assign(sc.fronts.size(), 0);
         out->cl.assign(sc.fronts.size(), 0);
+        out->tc.assign(sc.fronts.size(), 0);
         out->ms.assign(sc.fronts.size(), 1e30f);
         seen.assign(sc.fronts.size(), {});
       }
       for (size_t fi = 0; fi < sc.fronts.size() && s == LSW_OK; ++fi) {
-        const Front& f = sc.fronts[fi];
-        if (f.item_count <= 0 || f.slots_cap != r || f.cluster != cl) continue;   // shape did not fit here
-        const auto shape = std::make_tuple(f.item_count, f.max_slots, f.cluster);
-        float ms = 0.f;
-        auto hit = seen[fi].find(shape);
-        if (hit != seen[fi].end()) {
-          ms = hit->second;
-        } else {
-          // timed once; a short launch (where a first launch's overheads
-          // would show) is timed a second time and the smaller time kept
-          for (int rep = 0; rep < 2 && s == LSW_OK; ++rep) {
-            float t = 0.f;
-            if (cudaEventRecord(e0, st) != cudaSuccess) { s = fail(ctx, LSW_ERR_CUDA, "event"); break; }
-            if ((s = launch_front_of(ctx, &sc, fi, st)) != LSW_OK) break;
-            if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
-                cudaEventElapsedTime(&t, e0, e1) != cudaSuccess) {
-              s = fail(ctx, LSW_ERR_CUDA, "timing a sweep-front shape");
-              break;
+        for (int tc = 0; tc < 2 && s == LSW_OK; ++tc) {
+          Front& f = sc.fronts[fi];
+          if (f.item_count <= 0 || f.slots_cap != r || f.cluster != cl) continue;   // shape did not fit here
+          if (tc && !(tc_candidates(ctx) && tc_fits(ctx, f.max_slots, cl))) continue;
+          f.tc = tc != 0;
+          const auto shape = std::make_tuple(f.item_count, f.max_slots, f.cluster, tc);
+          float ms = 0.f;
+          auto hit = seen[fi].find(shape);
+          if (hit != seen[fi].end()) {
+            ms = hit->second;
+          } else {
+            // timed once; a short launch (where a first launch's overheads
+            // would show) is timed a second time and the smaller time kept
+            for (int rep = 0; rep < 2 && s == LSW_OK; ++rep) {
+              float t = 0.f;
+              if (cudaEventRecord(e0, st) != cudaSuccess) { s = fail(ctx, LSW_ERR_CUDA, "event"); break; }
+              if ((s = launch_front_of(ctx, &sc, fi, st)) != LSW_OK) break;
+              if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                  cudaEventElapsedTime(&t, e0, e1) != cudaSuccess) {
+                s = fail(ctx, LSW_ERR_CUDA, "timing a sweep-front shape");
+                break;
+              }
+              ms = rep == 0 ? t : std::min(ms, t);
+              if (t > 2.0f) break;
             }
-            ms = rep == 0 ? t : std::min(ms, t);
-            if (t > 2.0f) break;
+            if (s != LSW_OK) break;
+            seen[fi][shape] = ms;
           }
-          if (s != LSW_OK) break;
-          seen[fi][shape] = ms;
+          if (ms < out->ms[fi] * 0.99f) { out->ms[fi] = ms; out->r[fi] = r; out->cl[fi] = cl; out->tc[fi] = tc; }
         }
-        if (ms < out->ms[fi] * 0.99f) { out->ms[fi] = ms; out->r[fi] = r; out->cl[fi] = cl; }
       }
       if (s == LSW_OK) s = check_kernel_err(ctx, st);
     }
@@ -429,8 +453,13 @@ lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out, cudaStream_t st)
     }
     for (size_t fi = 0; fi < sc->fronts.size() && fi < tuned.r.size(); ++fi) {
       Front& f = sc->fronts[fi];
-      if (f.slots_cap == tuned.r[fi] && f.cluster == tuned.cl[fi]) f.tuned_ms = tuned.ms[fi];
+      if (f.slots_cap == tuned.r[fi] && f.cluster == tuned.cl[fi]) {
+        f.tuned_ms = tuned.ms[fi];
+        f.tc = fi < tuned.tc.size() && tuned.tc[fi] && tc_fits(ctx, f.max_slots, f.cluster);
+      }
     }
+    if (ctx->force_r > 0 && ctx->force_tc)
+      for (Front& f : sc->fronts) f.tc = f.item_count > 0 && tc_fits(ctx, f.max_slots, f.cluster);
     sc->nrhs = nrhs;
     std::unique_ptr<DevBuf[]> bufs(new DevBuf[3]);
     lsw_status s = upload_schedule(ctx, sc.get(), items, slots, groups, bufs.get());
@@ -478,6 +507,7 @@ lsw_status launch_front_of(lsw_ctx* ctx, const Schedule* sc, size_t fi, cudaStre
   a.item_count = i1 - i0;
   a.max_slots = f.max_slots;
   a.cluster = f.cluster;
+  a.tc = f.tc ? 1 : 0;
   cudaError_t e = ctx->prec != LSW_PREC_C128 ? launch_front<float>(a, ctx->max_ny, ctx->max_nx, st)
                                              : launch_front<double>(a, ctx->max_ny, ctx->max_nx, st);
   CK(e, "front kernel");
@@ -748,13 +778,19 @@ lsw_status lsw_ctx_create(lsw_ctx** out, int device) {
   if (const char* ev = std::getenv("LSW_SHIFT_STREAMS")) c->split_shifts = std::atoi(ev) != 0;
   // LSW_TUNE=0 leaves every sweep-front shape to the cost model
   if (const char* ev = std::getenv("LSW_TUNE")) c->tune = std::atoi(ev) != 0;
+  // LSW_SWEEP_TC=1 adds tensor-core line products to the complex64 tuning candidates
+  if (const char* ev = std::getenv("LSW_SWEEP_TC")) c->sweep_tc = std::atoi(ev) != 0;
   // LSW_FRONT_SHAPE=RxC imposes R slots per item (4, 8, 16) and C CTAs per half
   // chain (1, 2, 4) on every sweep front where that shape fits (no tuning)
   if (const char* ev = std::getenv("LSW_FRONT_SHAPE")) {
+    // (RxCt: with the line products on the tensor cores where they fit, complex64)
     int r = 0, cl = 0;
-    if (std::sscanf(ev, "%dx%d", &r, &cl) == 2 && (r == 4 || r == 8 || r == 16) && (cl == 1 || cl == 2 || cl == 4)) {
+    char t = 0;
+    const int got = std::sscanf(ev, "%dx%d%c", &r, &cl, &t);
+    if (got >= 2 && (r == 4 || r == 8 || r == 16) && (cl == 1 || cl == 2 || cl == 4)) {
       c->force_r = r;
       c->force_cl = cl;
+      c->force_tc = got == 3 && t == 't';
     }
   }
   {
@@ -825,6 +861,7 @@ lsw_status lsw_front_shapes(lsw_ctx* ctx, int nrhs, lsw_front_shape* out, int ca
     out[i].slots_cap = f.slots_cap;
     out[i].cluster = f.cluster;
     out[i].tuned_ms = f.tuned_ms;
+    out[i].tensor_cores = f.tc ? 1 : 0;
   }
   if (tune_seconds) *tune_seconds = ctx->tune_seconds;
   return LSW_OK;
@@ -1468,6 +1505,13 @@ lsw_status lsw_gmres(lsw_ctx* ctx, const void* b, void* x, int nrhs, const lsw_g
   const size_t budget = fr + held > margin ? fr + held - margin : 0;
   int chunk = (int)std::max<long long>(1, std::min<long long>(nrhs, (long long)(budget / per_rhs)));
   if (ctx->krylov_batch > 0) chunk = std::min(chunk, ctx->krylov_batch);
+  // sub-batches of equal size (64 as 32 + 32, not 54 + 10): every sweep
+  // launch of a sub-batch keeps as many right-hand sides as the others, and
+  // all sub-batches share one schedule
+  {
+    const int nsub = (nrhs + chunk - 1) / chunk;
+    chunk = (nrhs + nsub - 1) / nsub;
+  }
   lsw_gmres_report sub{}, acc{};
   acc.converged = 1;
   double tr = 0.0;

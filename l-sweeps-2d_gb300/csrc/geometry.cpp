@@ -379,7 +379,8 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
           it.group_count++;
         }
         it.slot_count = count;
-        it.scratch_off = (long long)(cl.nx + 1) * front_rpad(it.slot_count) * cl.ny;   // its size, for now
+        const int rs = plan.tc_scratch ? std::max(front_rpad(count), front_tc_slots(count)) : front_rpad(count);
+        it.scratch_off = (long long)(cl.nx + 1) * rs * cl.ny;   // its size, for now
         F.max_slots = std::max(F.max_slots, it.slot_count);
         items.push_back(it);
         F.item_count++;

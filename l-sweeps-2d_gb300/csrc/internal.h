@@ -96,6 +96,7 @@ struct Front {
   int cluster;            // CTAs per item chosen for this front
   int slots_cap = 0;      // slots per item at most (the planner's r)
   float tuned_ms = -1.f;  // the tuner's timing of this shape, -1 when the cost model chose it
+  bool tc = false;        // complex64 line products on the tensor cores
   bool mixed = false;     // an item mixes shifted decompositions: the front is one launch
   int sh_begin[5] = {0, 0, 0, 0, 0};   // items of shift s: [sh_begin[s], sh_begin[s + 1]) (not mixed)
 };
@@ -122,6 +123,9 @@ struct FrontPlan {
   // autotuner; an entry of 0, a missing entry or a shape that does not fit
   // leaves the front to the cost model
   std::vector<int> forced_r, forced_cl;
+  // items may run with tensor-core line products (8 or 16 slots, fewer
+  // padded): their forward storage is sized for that many slots
+  bool tc_scratch = false;
 };
 
 struct Schedule {
@@ -175,6 +179,7 @@ struct FrontArgs {
   int chunk;              // factor columns per streamed chunk (set by the launcher)
   int ksw;                // consumer column slices (set by the launcher)
   int split;              // factors hold bf16 hi/lo terms; the matvec runs on mma.sync
+  int tc;                 // complex64 line products on the tensor cores (tcgen05, 8 or 16 slots)
   long long wait_cycles;  // bounded-wait limit in clock cycles
 };
 // CTAs per half of an item (the item's cluster holds two halves) for a
@@ -191,7 +196,9 @@ int front_max_clusters(bool dbl, int cluster);
 int front_rmax(bool dbl);
 int front_rpad(int n);
 // bit CL (1, 2, 4) set where items of `slots` slots on clusters of 2 CL CTAs fit in shared memory
-int front_fit_mask(bool dbl, bool split, int max_ny, int max_nx, int slots);
+int front_fit_mask(bool dbl, bool split, int max_ny, int max_nx, int slots, bool tc = false);
+// slots of a tensor-core item (8 or 16) for items of at most n slots
+int front_tc_slots(int n);
 // split: write every factor entry as bf16 hi/lo terms; `prev` then holds the
 // previous FP32 block of each cell's two half chains (2 x ny x ldn complex per
 // cell) for the Schur recurrences.  lookahead: factor each next panel while

@@ -209,6 +209,82 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], unsigned a0, unsigned a1
                : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
+// ---- tensor-core (tcgen05) line products of complex64 items ----
+// A line's partial products D[row][n] = sum_k A[row][k] B[n][k] as real
+// GEMMs: A = the factor block with k = 2 column + (0: Re, 1: Im), B = the line
+// input with n = 2 slot + (0: Re, 1: Im) of the product, [x_re, -x_im] and
+// [x_im, x_re] along k; both split into three bf16 terms (hi + mid + lo, each
+// the rounded remainder of the previous ones) and multiplied as the six
+// products of combined order <= 2, FP32 accumulation in tensor memory.
+constexpr int kTcStages = 2;   // A operand stages, one k-block (8 columns, k = 16) each
+constexpr int kTcTile = 4096;  // one 128-row x 16-k bf16 tile of A, bytes
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// generic-proxy shared-memory writes of this thread visible to the tensor core
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// canonical K-major layout without swizzle: 8-row x 16-byte core matrices (8 k
+// each), k-adjacent core matrices 128 B apart.  A tiles [128 x 16]: 8-row
+// groups 256 B apart.  B [N x Kp] as k-tiles of 32 (N x 64 bytes each): 8-row
+// groups 512 B apart within a tile.
+__device__ __forceinline__ int a_off(int row, int k) {
+  return (row >> 3) * 256 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
+}
+__device__ __forceinline__ int b_off(int n, int k, int N) {
+  return (k >> 5) * (N * 64) + (n >> 3) * 512 + ((k & 31) >> 3) * 128 + (n & 7) * 16 + (k & 7) * 2;
+}
+// shared-memory matrix descriptor (start, leading byte offset 128, stride
+// byte offset `sbo`, in 16-byte units; descriptor version 1, no swizzle)
+__device__ __forceinline__ uint64_t tc_desc(unsigned addr, unsigned sbo) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+         (1ull << 46);
+}
+// (a, b) as three bf16x2 terms `term` bytes apart at byte offset `off`
+__device__ __forceinline__ void put3(unsigned char* base, int term, int off, float a, float b) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  const float ra = a - __low2float(h), rb = b - __high2float(h);
+  const __nv_bfloat162 m = __floats2bfloat162_rn(ra, rb);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(ra - __low2float(m), rb - __high2float(m));
+  *reinterpret_cast<__nv_bfloat162*>(base + off) = h;
+  *reinterpret_cast<__nv_bfloat162*>(base + term + off) = m;
+  *reinterpret_cast<__nv_bfloat162*>(base + 2 * term + off) = l;
+}
+// D (TMEM, FP32) = A B + (acc ? D : 0), A and B bf16 from shared memory
+__device__ __forceinline__ void tc_mma(unsigned d, uint64_t a, uint64_t b, unsigned idesc, unsigned acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+          d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+// N consecutive 32-bit TMEM columns of this thread's lane (N = 16 or 32)
+template <int N>
+__device__ __forceinline__ void tm_ld(unsigned taddr, float (&v)[N]) {
+  unsigned r[N];
+  if constexpr (N == 16) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+  } else {
+    static_assert(N == 32, "16 or 32 columns");
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+        "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+  }
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < N; ++j) v[j] = __uint_as_float(r[j]);
+}
+
 // CTA c of a cluster of CL owns rows/columns [c*ny/CL, (c+1)*ny/CL)
 __device__ __forceinline__ int owner_of(int row, int ny, int CL) { return ((row + 1) * CL - 1) / ny; }
 
@@ -292,9 +368,14 @@ template <> struct Pair<double> {
   __device__ __forceinline__ void load(const double2* p) { a = p[0]; b = p[1]; }
 };
 
-template <typename T, int R, bool SPLIT>
+template <typename T, int R, bool SPLIT, bool TCM = false>
 __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it, const DevCell& cl, unsigned char* smem) {
   using C = cx_t<T>;
+  // complex64 line products on the tensor cores (tcgen05, TMEM accumulators)
+  constexpr bool TC = TCM && !SPLIT && sizeof(T) == 4;
+  static_assert(!TC || R == 8 || R == 16, "tensor-core items carry 8 or 16 slots");
+  constexpr int TN = 2 * R;                                  // GEMM n: (slot, Re / Im)
+  constexpr int kTcCols = TN * 2 < 32 ? 32 : TN * 2;         // TMEM columns: two 128-row tiles
   const int CW = a.chunk;              // columns per chunk, multiple of 8
   const int KSW = a.ksw;               // column slices: consumer warps per row group
   static_assert((2 * kNSMax + 4) * 8 + 4 <= kHdr, "barrier header");
@@ -334,7 +415,7 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   // so that a warp keeps at most 8 slots of two rows in registers
   constexpr int SG = (!SPLIT && sizeof(T) == 4 && R > 8) ? 2 : 1;
   constexpr int RS = R / SG;
-  const int NCW = SPLIT ? (ny + 15) >> 4 : KSW * RG * SG;
+  const int NCW = TC ? kMaxRG * kMaxKSW : SPLIT ? (ny + 15) >> 4 : KSW * RG * SG;
   constexpr int NT = (2 * R + 7) / 8;   // split: n-tiles of 8 (Re, Im interleaved per slot)
   constexpr int NT8 = NT * 8;
   const int NCT = NCW * 32;
@@ -350,6 +431,10 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   uint64_t* exitb = pready + 2;         // cluster-wide "done with remote shared memory"
   uint64_t* xch = exitb + 1;            // the other half's last forward vector has landed in P
   volatile int* abort_flag = reinterpret_cast<volatile int*>(xch + 1);
+  // tensor-core items: A stage completions (tcgen05.commit), the TMEM address
+  static_assert((2 * kNSMax + 4) * 8 + 8 + 2 * 8 + 4 <= kHdr, "barrier header");
+  uint64_t* mmab = xch + 2;
+  unsigned* tslot = reinterpret_cast<unsigned*>(mmab + kTcStages);
   auto al16 = [](unsigned char* q) {
     return reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(q) + 15) & ~uintptr_t(15));
   };
@@ -383,7 +468,21 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   const size_t qbuf = (size_t)CL * qplane;
   p = al16(p + 2 * qbuf * sizeof(C));
   C* LS = reinterpret_cast<C*>(p);      // [KSW][R][64 RG] the column slices' partial sums, before their sum
-  if (!SPLIT) p = al16(p + (size_t)KSW * 64 * RG * R * sizeof(C));
+  if (!SPLIT && !TC) p = al16(p + (size_t)KSW * 64 * RG * R * sizeof(C));
+  // tensor-core items: the A stages ([stage][term][tile] 128 x 16 bf16) and the
+  // line input as B ([term] TN x Kp bf16, Kp = my columns x 2 rounded to 32)
+  const int MT = (ldn + 127) >> 7;
+  const int Kp = (2 * nJcap + 31) & ~31;
+  const int a_term = MT * kTcTile, b_term = TN * Kp * 2;
+  unsigned char* Ast = nullptr;
+  unsigned char* Bop = nullptr;
+  if constexpr (TC) {
+    p = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 127) & ~uintptr_t(127));
+    Ast = p;
+    p += (size_t)kTcStages * 3 * a_term;
+    Bop = p;
+    p = al16(p + (size_t)3 * b_term);
+  }
   // split: the next line's input as mma B words, hi and lo terms, [column][n]
   // with n = 2 slot + (0: real part, 1: imaginary part) of the product
   const int nJ8 = ((nJcap + 7) & ~7) + 8;
@@ -453,8 +552,28 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
     for (size_t i = tid; i < (size_t)NS * slot_elems; i += blockDim.x) ring[i] = czero<C>();
     for (size_t i = tid; i < 2 * (size_t)nJ8 * NT8; i += blockDim.x) BwH[i] = 0u;
   }
+  if constexpr (TC) {
+    // A rows past ldn and B columns past my columns are never written: zeros
+    // keep them without effect (the k-blocks of a chunk's last columns get
+    // zeros from the conversion)
+    uint4* z4 = reinterpret_cast<uint4*>(Ast);
+    const size_t n16 = ((size_t)kTcStages * 3 * a_term + (size_t)3 * b_term) / 16;
+    for (size_t i = tid; i < n16; i += blockDim.x) z4[i] = make_uint4(0u, 0u, 0u, 0u);
+    fence_async_smem();
+    if (warp == kAux) {   // the first consumer warp holds the accumulators' tensor memory
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(tslot)),
+                   "r"((unsigned)kTcCols)
+                   : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+      tc_fence_before();
+    }
+  }
   if (tid == 0) {
     *abort_flag = 0;
+    if constexpr (TC) {
+      mbar_init(&mmab[0], 1);
+      mbar_init(&mmab[1], 1);
+    }
     for (int i = 0; i < NS; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], NCW); }
     // one local arrive (with the expected bytes) per line; the partial sums
     // land by st.async and complete the transaction count
@@ -467,6 +586,7 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
+  if constexpr (TC) tc_fence_after();   // the TMEM address, after its allocation
   // every CTA's barriers are initialised before anyone arrives remotely
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 
@@ -656,6 +776,12 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
   // split: the mma B words of input entry e = (column, slot) of the next line,
   // n = 2 slot: (re, -im), n = 2 slot + 1: (im, re), hi and lo terms
   auto write_bw = [&](int e, C v) {
+    if constexpr (TC) {
+      // B rows n = 2 slot (Re of the product): [Re, -Im]; n = 2 slot + 1: [Im, Re]
+      const int jj = e / R, r = e - jj * R;
+      put3(Bop, b_term, b_off(2 * r, 2 * jj, TN), v.x, -v.y);
+      put3(Bop, b_term, b_off(2 * r + 1, 2 * jj, TN), v.y, v.x);
+    }
     if constexpr (SPLIT) {
       const int jj = e / R, r = e - jj * R;
       unsigned h0, l0, h1, l1;
@@ -675,12 +801,14 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
     V[e] = H[e];
     write_bw(e, H[e]);
   }
+  if constexpr (TC) fence_async_smem();
   named_sync(1, NSYNC);       // S0b
 
   // bytes of partial sums that land in my Q per line: my rows x R x CL CTAs
   const unsigned line_bytes = (unsigned)(nJ * R * CL * sizeof(C));
   if (CL > 1 && ct == 0) mbar_expect_tx(&pready[0], line_bytes);
   long long idx = 0;
+  int gkb = 0;                          // tensor-core items: k-blocks issued so far
   for (int li = 0; li < nline; ++li) {
     const int k = line_k(li);
     const int buf = li & 1;
@@ -689,7 +817,92 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
     // complete without this arrive)
     if (CL > 1 && ct == 0 && li + 1 < nline) mbar_expect_tx(&pready[(li + 1) & 1], line_bytes);
     C* Qb = Q + buf * qbuf;
-    if constexpr (SPLIT) {
+    if constexpr (TC) {
+      // ---- partial products of all rows with my columns on the tensor cores ----
+      // per k-block of 8 columns: the consumer warps convert the block's
+      // factor columns into the A stage, one thread issues the six products
+      // of each 128-row tile into TMEM and commits them to the stage's
+      // barrier; the next block is converted meanwhile into the other stage
+      const unsigned tb = *tslot;
+      // D FP32, A and B bf16, both K-major, N = TN, M = 128
+      constexpr unsigned idesc =
+          (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(TN >> 3) << 17) | ((unsigned)(128 >> 4) << 24);
+      int kb_line = 0;
+      for (int c = 0; c < nch; ++c, ++idx) {
+        const int slot = (int)(idx % NS);
+        const bool ok = mbar_wait<false>(&full[slot], (unsigned)((idx / NS) & 1), a.err, abort_flag, a.wait_cycles);
+        const C* S = ring + (size_t)slot * slot_elems;
+        const int c0 = c * CW;
+        const int ncol = min(CW, nJ - c0);
+        const int nkb = (ncol + 7) >> 3;
+        for (int kb = 0; kb < nkb; ++kb, ++gkb, ++kb_line) {
+          const int stg = gkb % kTcStages;
+          // the products that last read this stage are complete
+          if (gkb >= kTcStages)
+            mbar_wait<false>(&mmab[stg], (unsigned)(((gkb - kTcStages) / kTcStages) & 1), a.err, abort_flag,
+                             a.wait_cycles);
+          unsigned char* As = Ast + (size_t)stg * 3 * a_term;
+          // a warp pass: 8 rows x 4 columns, one 128-byte core-matrix row per term
+          for (int u = cw; u < MT * 32; u += NCW) {
+            const int row = (u >> 1) * 8 + (lane >> 2);
+            const int cq = (u & 1) * 4 + (lane & 3);   // column within the k-block
+            const int cc = kb * 8 + cq;                 // column within the chunk
+            C v = czero<C>();
+            if (ok && row < ldn && cc < ncol) v = S[(size_t)cc * ldn + row];
+            put3(As, a_term, (row >> 7) * kTcTile + a_off(row & 127, 2 * cq), v.x, v.y);
+          }
+          fence_async_smem();
+          named_sync(2, NCT);   // the stage is written
+          if (ct == 0) {
+            tc_fence_after();
+            const unsigned a0 = saddr(As), b0 = saddr(Bop);
+            const int kk = 2 * (c0 + kb * 8);   // the block's first k in B (a multiple of 16)
+            const unsigned bk = (unsigned)((kk >> 5) * (TN * 64) + ((kk >> 4) & 1) * 256);
+            for (int t = 0; t < MT; ++t) {
+#pragma unroll
+              for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j + i < 3; ++j)
+                  tc_mma(tb + (unsigned)(t * TN), tc_desc(a0 + (unsigned)(i * a_term + t * kTcTile), 256u),
+                         tc_desc(b0 + (unsigned)(j * b_term) + bk, 512u), idesc,
+                         (kb_line > 0 || i + j > 0) ? 1u : 0u);
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             saddr(&mmab[stg]))
+                         : "memory");
+          }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[slot]);
+      }
+      // the line's products are complete: each row's sums (lane r of tile t
+      // in TMEM) to the CTA of my half that owns the row
+      const int tq = cw >> 2;
+      if (tq < MT) {
+        mbar_wait<false>(&mmab[(gkb - 1) % kTcStages], (unsigned)(((gkb - 1) / kTcStages) & 1), a.err, abort_flag,
+                         a.wait_cycles);
+        tc_fence_after();
+        float d[TN];
+        tm_ld<TN>(tb + ((unsigned)((cw & 3) * 32) << 16) + (unsigned)(tq * TN), d);
+        tc_fence_before();
+        const int row = tq * 128 + (cw & 3) * 32 + lane;
+        if (row < ny) {
+          const int info = rowinfo[row];
+          C* dst = Qb + ((size_t)crank * nJcap + (info & 0xffff)) * R;
+#pragma unroll
+          for (int q2 = 0; q2 < R / 2; ++q2) {
+            const C v0 = make_float2(d[4 * q2], d[4 * q2 + 1]);
+            const C v1 = make_float2(d[4 * q2 + 2], d[4 * q2 + 3]);
+            if (CL == 1) {
+              dst[2 * q2] = v0;
+              dst[2 * q2 + 1] = v1;
+            } else {
+              st_async2(dst + 2 * q2, (unsigned)(info >> 16), v0, v1, &pready[buf]);
+            }
+          }
+        }
+      }
+    } else if constexpr (SPLIT) {
       // ---- tensor-core partial products: my 16-row m-tile with all my columns ----
       // A (factor, bf16 hi/lo words, column-major) x B (next input, [column][n])
       // on mma.sync m16n8k16: three products hi*hi + hi*lo + lo*hi per k-step
@@ -873,9 +1086,22 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
         write_bw(e, x);
       }
     }
+    if constexpr (TC) fence_async_smem();   // the B words, for the next line's products
     named_sync(1, NSYNC);     // sync2: V holds the next line's input
   }
   named_sync(1, NSYNC);       // every x_k is stored
+  if constexpr (TC) {
+    if (cw == 0) {
+      // every product has completed (each line's were waited for before its
+      // results were read; the wait below returns at once unless one ran out)
+      if (gkb > 0)
+        mbar_wait<false>(&mmab[(gkb - 1) % kTcStages], (unsigned)(((gkb - 1) / kTcStages) & 1), a.err, nullptr,
+                         a.wait_cycles);
+      tc_fence_after();
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(*tslot), "r"((unsigned)kTcCols)
+                   : "memory");
+    }
+  }
   epilogue(ct);
 
   {
@@ -889,13 +1115,17 @@ __device__ __forceinline__ void front_body(const FrontArgs& a, const DevItem& it
 }
 
 // 16 warps (4 auxiliary + up to 3 row groups x 4 column slices) x 128 registers
-template <typename T, bool SPLIT>
+template <typename T, bool SPLIT, bool TCM = false>
 __global__ void __maxnreg__(128) k_front(FrontArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const DevItem it = a.items[blockIdx.x / (2 * a.cluster)];
   const DevCell cl = a.cells[it.cell];
   const int n = it.slot_count;
-  if constexpr (sizeof(T) == 4) {
+  if constexpr (TCM) {
+    // tensor-core items: 8 or 16 slots (fewer pad with empty slots)
+    if (n <= 8) front_body<T, 8, false, true>(a, it, cl, smem);
+    else front_body<T, 16, false, true>(a, it, cl, smem);
+  } else if constexpr (sizeof(T) == 4) {
     if (n <= 1) front_body<T, 1, SPLIT>(a, it, cl, smem);
     else if (n <= 2) front_body<T, 2, SPLIT>(a, it, cl, smem);
     else if (n <= 4) front_body<T, 4, SPLIT>(a, it, cl, smem);
@@ -911,10 +1141,15 @@ __global__ void __maxnreg__(128) k_front(FrontArgs a) {
 }
 
 template <typename T>
-size_t smem_need(int ldn_max, int ny_max, int nx_max, int R, int KSW, int CL, int CW, int NS, bool split) {
+size_t smem_need(int ldn_max, int ny_max, int nx_max, int R, int KSW, int CL, int CW, int NS, bool split,
+                 bool tc = false) {
   using C = cx_t<T>;
   const int nJ = (ny_max + CL - 1) / CL + 1;
+  // tensor-core items: A stages and the three B terms (+ alignment) instead of the slices' staging
+  const size_t tc_bytes = (size_t)kTcStages * 3 * ((ldn_max + 127) / 128) * kTcTile +
+                          (size_t)3 * 2 * R * ((2 * nJ + 31) & ~31) * 2 + 128;
   const size_t staging = split ? 2 * (size_t)(((nJ + 7) & ~7) + 8) * (8 * ((2 * R + 7) / 8)) * sizeof(unsigned)
+                         : tc  ? tc_bytes
                                : (size_t)KSW * 64 * kMaxRG * R * sizeof(C);
   return kHdr + (size_t)NS * CW * ldn_max * sizeof(C) + 4 * (size_t)R * nJ * sizeof(C) + nx_max + nJ + 32 +
          2 * (size_t)CL * R * nJ * sizeof(C) + staging + 4 * (size_t)ny_max +
@@ -925,6 +1160,7 @@ size_t smem_need(int ldn_max, int ny_max, int nx_max, int R, int KSW, int CL, in
 }  // namespace
 
 int front_rmax(bool dbl) { return dbl ? 8 : 16; }
+int front_tc_slots(int n) { return n <= 8 ? 8 : 16; }
 int front_rpad(int n) { return n <= 1 ? 1 : n <= 2 ? 2 : n <= 4 ? 4 : n <= 8 ? 8 : n <= 12 ? 12 : 16; }
 
 namespace {
@@ -933,8 +1169,10 @@ namespace {
 // R slots on clusters of 2 CL CTAs; false if nothing fits in shared memory.
 template <typename T>
 bool front_shape(int max_ny, int max_nx, int R, int CL, bool split, int maxopt, int* ldn_out, int* ksw_out,
-                 int* cw_out, int* ns_out, size_t* smem_out) {
+                 int* cw_out, int* ns_out, size_t* smem_out, bool tc = false) {
   int ldn = (max_ny + 3) & ~3;
+  // tensor-core items: complex64, 8 or 16 slots, at most two 128-row tiles
+  if (tc && (split || sizeof(T) != 4 || (R != 8 && R != 16) || ldn > 256)) return false;
   if (split) {   // the split factor layout's column stride (4 mod 8)
     ldn = max_ny;
     while (ldn % 8 != 4) ++ldn;
@@ -946,7 +1184,7 @@ bool front_shape(int max_ny, int max_nx, int R, int CL, bool split, int maxopt, 
   int KSW = kMaxKSW;
   // (complex64 with more than 8 slots: two slot groups, so at most 2 slices)
   const int sgroups = (!split && sizeof(T) == 4 && R > 8) ? 2 : 1;
-  while (KSW > 1 && (split || nJmax < 4 * KSW || KSW * sgroups > kMaxKSW ||
+  while (KSW > 1 && (split || tc || nJmax < 4 * KSW || KSW * sgroups > kMaxKSW ||
                      (size_t)KSW * 64 * kMaxRG * R * sizeof(cx_t<T>) > 65536))
     --KSW;
   const int cwmax = (int)std::min<size_t>(((size_t)65536 / ((size_t)ldn * sizeof(cx_t<T>))) & ~size_t(7),
@@ -954,27 +1192,27 @@ bool front_shape(int max_ny, int max_nx, int R, int CL, bool split, int maxopt, 
   int CW = std::max(8, cwmax), NS = 0;
   for (; CW >= 8; CW -= 8) {
     for (NS = 4; NS >= 2; --NS)
-      if (smem_need<T>(ldn, max_ny, max_nx, R, KSW, CL, CW, NS, split) <= (size_t)maxopt) break;
+      if (smem_need<T>(ldn, max_ny, max_nx, R, KSW, CL, CW, NS, split, tc) <= (size_t)maxopt) break;
     if (NS >= 2) break;
   }
   if (CW < 8) return false;
   *ldn_out = ldn; *ksw_out = KSW; *cw_out = CW; *ns_out = NS;
-  *smem_out = smem_need<T>(ldn, max_ny, max_nx, R, KSW, CL, CW, NS, split);
+  *smem_out = smem_need<T>(ldn, max_ny, max_nx, R, KSW, CL, CW, NS, split, tc);
   return true;
 }
 
 }  // namespace
 
-int front_fit_mask(bool dbl, bool split, int max_ny, int max_nx, int slots) {
+int front_fit_mask(bool dbl, bool split, int max_ny, int max_nx, int slots, bool tc) {
   int dev = 0, maxopt = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const int R = std::min(front_rpad(std::max(1, slots)), front_rmax(dbl));
+  const int R = tc ? front_tc_slots(slots) : std::min(front_rpad(std::max(1, slots)), front_rmax(dbl));
   int mask = 0, ldn, ksw, cw, ns;
   size_t smem;
   for (int cl = 1; cl <= 4; cl *= 2) {
-    const bool ok = dbl ? front_shape<double>(max_ny, max_nx, R, cl, split, maxopt, &ldn, &ksw, &cw, &ns, &smem)
-                        : front_shape<float>(max_ny, max_nx, R, cl, split, maxopt, &ldn, &ksw, &cw, &ns, &smem);
+    const bool ok = dbl ? front_shape<double>(max_ny, max_nx, R, cl, split, maxopt, &ldn, &ksw, &cw, &ns, &smem, tc)
+                        : front_shape<float>(max_ny, max_nx, R, cl, split, maxopt, &ldn, &ksw, &cw, &ns, &smem, tc);
     if (ok) mask |= 1 << cl;
   }
   return mask;
@@ -987,7 +1225,9 @@ cudaError_t launch_front(const FrontArgs& a_in, int max_ny, int max_nx, cudaStre
   const bool dbl = sizeof(T) == 8;
   const bool split = a.split != 0;
   if (split && dbl) return cudaErrorInvalidValue;
-  const int R = std::min(front_rpad(std::max(1, a.max_slots)), front_rmax(dbl));
+  const bool tc = a.tc != 0;
+  if (tc && (dbl || split || a.max_slots > 16)) return cudaErrorInvalidValue;
+  const int R = tc ? front_tc_slots(a.max_slots) : std::min(front_rpad(std::max(1, a.max_slots)), front_rmax(dbl));
   if (a.cluster < 1) a.cluster = 1;
   if (a.cluster > 4 || max_nx < 5) return cudaErrorInvalidValue;   // clusters of <= 8; two lines per half
   int dev = 0, maxopt = 0;
@@ -995,7 +1235,7 @@ cudaError_t launch_front(const FrontArgs& a_in, int max_ny, int max_nx, cudaStre
   cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   int ldn = 0, KSW = 0, CW = 0, NS = 0;
   size_t smem = 0;
-  if (!front_shape<T>(max_ny, max_nx, R, a.cluster, split, maxopt, &ldn, &KSW, &CW, &NS, &smem))
+  if (!front_shape<T>(max_ny, max_nx, R, a.cluster, split, maxopt, &ldn, &KSW, &CW, &NS, &smem, tc))
     return cudaErrorInvalidConfiguration;
   a.ksw = KSW;
   a.stages = NS;
@@ -1011,16 +1251,17 @@ cudaError_t launch_front(const FrontArgs& a_in, int max_ny, int max_nx, cudaStre
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  auto kern = split ? k_front<float, true> : k_front<T, false>;
+  void (*kern)(FrontArgs) = k_front<T, false>;
+  if constexpr (sizeof(T) == 4) {
+    if (split) kern = k_front<float, true>;
+    else if (tc) kern = k_front<float, false, true>;
+  }
   // the attribute is an upper bound: always the device maximum, so that
   // host threads launching concurrently never lower it under one another
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, maxopt);
   if (e != cudaSuccess) return e;
   cfg.blockDim = dim3(32 * (kAux + kMaxRG * kMaxKSW));
-  if constexpr (sizeof(T) == 4) {
-    if (split) return cudaLaunchKernelEx(&cfg, k_front<float, true>, a);
-  }
-  return cudaLaunchKernelEx(&cfg, k_front<T, false>, a);
+  return cudaLaunchKernelEx(&cfg, kern, a);
 }
 
 int front_max_clusters(bool dbl, int cluster) {

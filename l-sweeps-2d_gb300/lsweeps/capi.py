@@ -58,7 +58,7 @@ class CellInfo(C.Structure):
 
 class FrontShape(C.Structure):
     _fields_ = [("items", C.c_int), ("max_slots", C.c_int), ("slots_cap", C.c_int), ("cluster", C.c_int),
-                ("tuned_ms", C.c_float)]
+                ("tuned_ms", C.c_float), ("tensor_cores", C.c_int)]
 
 
 class GmresOpts(C.Structure):
