@@ -297,7 +297,9 @@ lsw_status lsw_local_solve(lsw_ctx* ctx, int cell, const void* b_dev, void* x_de
  * All calls share the array: calls that overlap on the GPU (other streams,
  * other contexts on the same device) race and must be serialised by the
  * caller.  Nothing in the array needs clearing between calls: every element
- * is written before it is read. */
+ * is written before it is read.  Like lsw_local_solve, the call reads the
+ * kernels' error word back and synchronises `stream` before it returns, so it
+ * cannot be recorded into a CUDA graph (stream capture). */
 lsw_status lsw_local_solve_noalloc(lsw_ctx* ctx, int cell, const void* b_dev, void* x_dev, int nrhs,
                                    void* stream);
 
