@@ -375,9 +375,21 @@ def run_gpu(args):
     model_shapes, _ = S.front_shapes(nrhs)
     S.set_tuning(True)
     apply_ms(1)
+    # with per-sweep launches (a single right-hand side): the apply with one
+    # launch per sweep step beside it, on the same context
+    steps_per_apply = 3 * spec.N - 3
+    t_step_graph = None
+    if len(shapes) > steps_per_apply:
+        S.set_sweep_lanes(0)
+        S.front_shapes(nrhs)
+        t_step_graph = apply_ms()
+        S.set_sweep_lanes(nrhs)
+        apply_ms(1)
     launch = {
         "apply_ms_tuned_graph": t_tuned_graph, "apply_ms_tuned_eager": t_tuned_eager,
         "apply_ms_model_graph": t_model_graph, "tune_s": tune_s,
+        "per_sweep_launches": len(shapes) > steps_per_apply, "launches_per_apply": len(shapes),
+        "apply_ms_one_launch_per_step_graph": t_step_graph,
         "fronts_changed_by_tuner": sum(1 for a, b in zip(shapes, model_shapes)
                                        if (a["slots_cap"], a["cluster"]) != (b["slots_cap"], b["cluster"])),
         "tuned_shapes": " ".join(f"{f['slots_cap']}x{f['cluster']}" for f in shapes),
@@ -504,14 +516,29 @@ def run_apply_only(args):
         torch.cuda.synchronize()
         ts.append(e0.elapsed_time(e1))
     line = {"apply_only": args.config, "precision": prec, "nrhs": args.nrhs,
-            "applies": args.warmup + args.steps, "fronts_per_apply": 3 * spec.N - 3 + 1,
-            "tune_s": round(tune_s, 2),
+            "applies": args.warmup + args.steps, "steps_per_apply": 3 * spec.N - 3,
+            "launches_per_apply": len(shapes), "tune_s": round(tune_s, 2),
             "shapes": " ".join("%dx%d%s" % (f["slots_cap"], f["cluster"], "t" if f["tensor_cores"] else "")
                                for f in shapes)}
     if ts:
         # graph-replayed applies, CUDA events on the launching stream
         med_ms = statistics.median(ts)
         line.update({"apply_ms": round(med_ms, 3), "apply_ms_per_rhs": round(med_ms / args.nrhs, 3)})
+        if len(shapes) > 3 * spec.N - 3:
+            # per-sweep launches: the same applies with one launch per sweep step
+            S.set_sweep_lanes(0)
+            S.front_shapes(args.nrhs)
+            S.apply_precond(v, out=y)
+            t1 = []
+            for _ in range(args.steps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                S.apply_precond(v, out=y)
+                e1.record(st)
+                torch.cuda.synchronize()
+                t1.append(e0.elapsed_time(e1))
+            line["apply_ms_one_launch_per_step"] = round(statistics.median(t1), 3)
+            S.set_sweep_lanes(args.nrhs)
     if args.warmup + args.steps > 0:
         # the algorithmic and streamed bytes of one apply (one more, profiled, apply)
         _, pr = S.apply_precond_profiled(v)

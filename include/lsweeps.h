@@ -181,6 +181,22 @@ lsw_status lsw_ctx_set_graphs(lsw_ctx* ctx, int enable);
  * reference (its sweeps are host loops, DDCheckerboard.cpp:812-880). */
 lsw_status lsw_ctx_set_tuning(lsw_ctx* ctx, int enable);
 
+/* Per-sweep launches for batches of at most `max_rhs` right-hand sides (1,
+ * the default; LSW_SWEEP_LANES=<n> in the environment at context creation
+ * sets it; 0 turns them off).  Such a batch runs every stage-2 sweep and every
+ * L-sweep of the preconditioner as its own chain of launches on its own
+ * stream, an L-sweep's step dd after its two producing stage-2 sweeps have
+ * passed column / row dd + 1, so the L-sweeps start while stage 2 still runs
+ * and the sweeps fill the GPU between one another's launches; their outputs go
+ * to one plane per stage-2 sweep, summed at the end (four times the output
+ * pool of one launch per step).  Results equal those of one launch per step up
+ * to the order of the final sums.  Their launch shapes come from the cost
+ * model (launches timed alone do not show how they share the GPU).  Changing
+ * the setting drops the context's schedules (rebuilt on next use; waits for
+ * the device).  No counterpart in the reference (its sweeps are host loops,
+ * DDCheckerboard.cpp:812-880). */
+lsw_status lsw_ctx_set_sweep_lanes(lsw_ctx* ctx, int max_rhs);
+
 typedef struct {
   int items;        /* items (cluster launches) in the front */
   int max_slots;    /* slots of the largest item */
@@ -192,7 +208,9 @@ typedef struct {
 
 /* The launch shapes of the sweep fronts of a batch of nrhs right-hand sides
  * (building, and with tuning on measuring, the schedule if this batch size has
- * none yet, on `stream`): up to `capacity` entries in `out`, the front count in
+ * none yet, on `stream`): up to `capacity` entries in `out` (in launch order;
+ * with per-sweep launches stage 1, then per stage-2 column the four sweeps,
+ * then per stage-3 anti-diagonal the four L-sweeps), the launch count in
  * *n_fronts, the context's total tuning time so far in *tune_seconds (may be
  * NULL).  Requires a factorised problem. */
 lsw_status lsw_front_shapes(lsw_ctx* ctx, int nrhs, lsw_front_shape* out, int capacity, int* n_fronts,

@@ -89,6 +89,14 @@ struct lsw_ctx {
   bool split_shifts = true;
   cudaStream_t side[3] = {nullptr, nullptr, nullptr};
   cudaEvent_t side_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // batches of at most this many right-hand sides run every stage-2 and
+  // stage-3 sweep as its own chain of launches (one stream per sweep, created
+  // on first use; events per stage-2 launch for the L-sweeps' waits)
+  int lanes_max_rhs = 1;
+  cudaStream_t lane_st[8] = {};
+  cudaEvent_t lane_fork = nullptr;
+  cudaEvent_t lane_join[8] = {};
+  std::vector<cudaEvent_t> lane_ev;   // [sweep 0..3][t 0..N-1]
   // bounded-wait limit of the sweep and factorisation kernels, in SM clock cycles
   long long wait_cycles = 4000000000LL;   // ~2 s at 2 GHz
   // device address of the allocation-free solve's fixed scratch array on this
@@ -123,6 +131,13 @@ struct lsw_ctx {
       if (q) cudaStreamDestroy(q);
     for (auto& e : side_ev)
       if (e) cudaEventDestroy(e);
+    for (auto& q : lane_st)
+      if (q) cudaStreamDestroy(q);
+    for (auto& e : lane_join)
+      if (e) cudaEventDestroy(e);
+    for (auto& e : lane_ev)
+      if (e) cudaEventDestroy(e);
+    if (lane_fork) cudaEventDestroy(lane_fork);
   }
 };
 
@@ -252,10 +267,10 @@ lsw_status upload_schedule(lsw_ctx* ctx, Schedule* sc, const std::vector<DevItem
 }
 
 // the trace, output and scratch pools of a batch of nrhs right-hand sides
-lsw_status ensure_pools(lsw_ctx* ctx, int nrhs, long long scratch_elems) {
+lsw_status ensure_pools(lsw_ctx* ctx, int nrhs, long long scratch_elems, int planes) {
   const size_t cs = csize(ctx->prec);
   CK(ctx->d_traces.ensure((size_t)nrhs * 4 * ctx->ncell * 24 * ctx->LP * cs), "cudaMalloc(traces)");
-  CK(ctx->d_outs.ensure((size_t)nrhs * 4 * ctx->n2 * cs), "cudaMalloc(outs)");
+  CK(ctx->d_outs.ensure((size_t)nrhs * planes * 4 * ctx->n2 * cs), "cudaMalloc(outs)");
   CK(ctx->d_scratch.ensure(std::max<size_t>(1, (size_t)scratch_elems * cs)), "cudaMalloc(scratch)");
   return LSW_OK;
 }
@@ -352,8 +367,8 @@ lsw_status tune_fronts(lsw_ctx* ctx, int nrhs, const FrontPlan& plan, cudaStream
     for (int cl = 1; cl <= plan.cluster_cap && s == LSW_OK; cl *= 2) {
       if (cl > 1 && plan.max_clusters[cl] <= 0) continue;
       FrontPlan p = plan;
-      p.forced_r.assign(8 * (size_t)ctx->N + 8, r);
-      p.forced_cl.assign(8 * (size_t)ctx->N + 8, cl);
+      p.forced_r.assign(16 * (size_t)ctx->N + 16, r);
+      p.forced_cl.assign(16 * (size_t)ctx->N + 16, cl);
       Schedule sc;
       std::vector<DevItem> items; std::vector<DevSlot> slots; std::vector<DevGroup> groups;
       try {
@@ -362,7 +377,7 @@ lsw_status tune_fronts(lsw_ctx* ctx, int nrhs, const FrontPlan& plan, cudaStream
         continue;
       }
       if ((s = upload_schedule(ctx, &sc, items, slots, groups, bufs)) != LSW_OK) break;
-      if ((s = ensure_pools(ctx, nrhs, sc.scratch_elems)) != LSW_OK) break;
+      if ((s = ensure_pools(ctx, nrhs, sc.scratch_elems, 1)) != LSW_OK) break;
       if (out->r.empty()) {
         out->r.assign(sc.fronts.size(), 0);
         out->cl.assign(sc.fronts.size(), 0);
@@ -426,11 +441,14 @@ lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out, cudaStream_t st)
     } catch (const std::exception& ex) {
       return fail(ctx, LSW_ERR_UNSUPPORTED, ex.what());
     }
+    plan.lanes = nrhs <= ctx->lanes_max_rhs;
     TuneEntry tuned;
     if (ctx->force_r > 0) {
-      plan.forced_r.assign(8 * (size_t)ctx->N + 8, ctx->force_r);
-      plan.forced_cl.assign(8 * (size_t)ctx->N + 8, ctx->force_cl);
-    } else if (ctx->tune && ctx->factorized) {
+      plan.forced_r.assign(16 * (size_t)ctx->N + 16, ctx->force_r);
+      plan.forced_cl.assign(16 * (size_t)ctx->N + 16, ctx->force_cl);
+    } else if (ctx->tune && ctx->factorized && !plan.lanes) {
+      // (per-sweep launches run concurrently with one another, which a launch
+      // timed alone does not show: their shapes come from the cost model)
       std::lock_guard<std::mutex> lk(g_tune_mu);
       tune_file_read();
       const std::string key = tune_key(ctx, nrhs);
@@ -461,6 +479,7 @@ lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out, cudaStream_t st)
     if (ctx->force_r > 0 && ctx->force_tc)
       for (Front& f : sc->fronts) f.tc = f.item_count > 0 && tc_fits(ctx, f.max_slots, f.cluster);
     sc->nrhs = nrhs;
+    sc->lanes = plan.lanes;
     std::unique_ptr<DevBuf[]> bufs(new DevBuf[3]);
     lsw_status s = upload_schedule(ctx, sc.get(), items, slots, groups, bufs.get());
     if (s != LSW_OK) return s;
@@ -468,7 +487,7 @@ lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out, cudaStream_t st)
     it = ctx->sched.emplace(nrhs, std::move(sc)).first;
   }
   Schedule* sc = it->second.get();
-  lsw_status s = ensure_pools(ctx, nrhs, sc->scratch_elems);
+  lsw_status s = ensure_pools(ctx, nrhs, sc->scratch_elems, sc->lanes ? kLanePlanes : 1);
   if (s != LSW_OK) return s;
   if (before[0] != ctx->d_traces.p || before[1] != ctx->d_outs.p || before[2] != ctx->d_scratch.p) {
     // the captured applies point at the old pools
@@ -514,6 +533,70 @@ lsw_status launch_front_of(lsw_ctx* ctx, const Schedule* sc, size_t fi, cudaStre
   return LSW_OK;
 }
 
+// Per-sweep launches (sc->lanes): stage 1 on st; then each stage-2 sweep on
+// its own stream, every launch recording an event, and each L-sweep on its own
+// stream, its step dd waiting first for the events of its two producing
+// stage-2 sweeps at front min(dd + 1, N - 1) (see kLanePlanes); every stream
+// joins st before the sum.  With `streams` false (per-front timing) the
+// launches run on st in schedule order, a topological order of the same
+// dependencies.  Either way each output value and trace line sees the same
+// writes in the same order, so the results are identical.
+lsw_status enqueue_lanes(lsw_ctx* ctx, Schedule* sc, cudaStream_t st, int* k, bool streams) {
+  lsw_status s;
+  if (!streams) {
+    for (size_t fi = 0; fi < sc->fronts.size(); ++fi) {
+      if (ctx->front_events) CK(cudaEventRecord((*ctx->front_events)[2 * fi], st), "event");
+      if ((s = launch_front_of(ctx, sc, fi, st)) != LSW_OK) return s;
+      if (ctx->front_events) CK(cudaEventRecord((*ctx->front_events)[2 * fi + 1], st), "event");
+      *k += sc->fronts[fi].item_count > 0 ? 1 : 0;
+    }
+    return LSW_OK;
+  }
+  const int N = ctx->N;
+  for (int l = 0; l < 8; ++l) {
+    if (!ctx->lane_st[l]) CK(cudaStreamCreateWithFlags(&ctx->lane_st[l], cudaStreamNonBlocking), "sweep stream");
+    if (!ctx->lane_join[l]) CK(cudaEventCreateWithFlags(&ctx->lane_join[l], cudaEventDisableTiming), "sweep event");
+  }
+  if (!ctx->lane_fork) CK(cudaEventCreateWithFlags(&ctx->lane_fork, cudaEventDisableTiming), "sweep event");
+  if ((int)ctx->lane_ev.size() != 4 * N) {
+    for (auto& e : ctx->lane_ev)
+      if (e) cudaEventDestroy(e);
+    ctx->lane_ev.assign(4 * (size_t)N, nullptr);
+    for (auto& e : ctx->lane_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "sweep event");
+  }
+  size_t fi = 0;
+  for (; fi < sc->fronts.size() && sc->fronts[fi].lane < 0; ++fi) {   // stage 1
+    if ((s = launch_front_of(ctx, sc, fi, st)) != LSW_OK) return s;
+    *k += sc->fronts[fi].item_count > 0 ? 1 : 0;
+  }
+  CK(cudaEventRecord(ctx->lane_fork, st), "fork");
+  for (int l = 0; l < 8; ++l) CK(cudaStreamWaitEvent(ctx->lane_st[l], ctx->lane_fork, 0), "fork wait");
+  int waited[4] = {0, 0, 0, 0};   // per L-sweep: the stage-2 front it last waited for
+  for (; fi < sc->fronts.size(); ++fi) {
+    const Front& f = sc->fronts[fi];
+    if (f.lane < 0) return fail(ctx, LSW_ERR_CUDA, "per-sweep schedule out of order");
+    cudaStream_t q = ctx->lane_st[f.lane];
+    if (f.stage == 3) {
+      const int w = f.lane - 4, t = std::min(f.step + 1, N - 1);
+      if (t > waited[w]) {
+        CK(cudaStreamWaitEvent(q, ctx->lane_ev[(size_t)kLaneProducerLR[w] * N + t], 0), "sweep wait");
+        CK(cudaStreamWaitEvent(q, ctx->lane_ev[(size_t)kLaneProducerUD[w] * N + t], 0), "sweep wait");
+        waited[w] = t;
+      }
+    }
+    if (f.item_count > 0) {
+      if ((s = launch_front_of(ctx, sc, fi, q)) != LSW_OK) return s;
+      ++*k;
+    }
+    if (f.stage == 2) CK(cudaEventRecord(ctx->lane_ev[(size_t)f.lane * N + f.step], q), "sweep event");
+  }
+  for (int l = 0; l < 8; ++l) {
+    CK(cudaEventRecord(ctx->lane_join[l], ctx->lane_st[l]), "join");
+    CK(cudaStreamWaitEvent(st, ctx->lane_join[l], 0), "join wait");
+  }
+  return LSW_OK;
+}
+
 // The launches of one apply on stream st: clear the trace and output pools,
 // every sweep front, the sum of the four shifted outputs.  The input and
 // output addresses are read from ctx->d_ref (set by the caller beforehand),
@@ -525,13 +608,19 @@ lsw_status launch_front_of(lsw_ctx* ctx, const Schedule* sc, size_t fi, cudaStre
 // their outputs are summed, so the launches of one shift's next front start
 // while other shifts still run, and the ends of the fronts overlap instead of
 // leaving SMs idle.  A mixed front joins every stream and runs alone.
+// Per-sweep schedules (sc->lanes) run on the sweep streams of enqueue_lanes,
+// captured or not (one stream when the fronts are timed one by one).
 lsw_status enqueue_apply(lsw_ctx* ctx, Schedule* sc, int nrhs, cudaStream_t st, int* kernels,
                          bool split_shifts = false) {
   const size_t cs = csize(ctx->prec);
+  const int planes = sc->lanes ? kLanePlanes : 1;
   CK(cudaMemsetAsync(ctx->d_traces.p, 0, (size_t)nrhs * 4 * ctx->ncell * 24 * ctx->LP * cs, st), "memset traces");
-  CK(cudaMemsetAsync(ctx->d_outs.p, 0, (size_t)nrhs * 4 * ctx->n2 * cs, st), "memset outs");
+  CK(cudaMemsetAsync(ctx->d_outs.p, 0, (size_t)nrhs * planes * 4 * ctx->n2 * cs, st), "memset outs");
   int k = 0;
-  if (split_shifts) {
+  if (sc->lanes) {
+    lsw_status s = enqueue_lanes(ctx, sc, st, &k, ctx->front_events == nullptr);
+    if (s != LSW_OK) return s;
+  } else if (split_shifts) {
     for (int i = 0; i < 3; ++i)
       if (!ctx->side[i]) CK(cudaStreamCreateWithFlags(&ctx->side[i], cudaStreamNonBlocking), "side stream");
     for (int i = 0; i < 4; ++i)
@@ -580,8 +669,9 @@ lsw_status enqueue_apply(lsw_ctx* ctx, Schedule* sc, int nrhs, cudaStream_t st, 
     }
   }
   double2* const* yref = reinterpret_cast<double2* const*>(ctx->d_ref.p) + 1;
-  cudaError_t e = ctx->prec != LSW_PREC_C128 ? launch_combine_ref<float>(ctx->d_outs.p, yref, nrhs, ctx->n2, st)
-                                             : launch_combine_ref<double>(ctx->d_outs.p, yref, nrhs, ctx->n2, st);
+  cudaError_t e = ctx->prec != LSW_PREC_C128
+                      ? launch_combine_ref<float>(ctx->d_outs.p, yref, nrhs, ctx->n2, planes, st)
+                      : launch_combine_ref<double>(ctx->d_outs.p, yref, nrhs, ctx->n2, planes, st);
   CK(e, "combine kernel");
   *kernels = k + 1;
   return LSW_OK;
@@ -776,6 +866,8 @@ lsw_status lsw_ctx_create(lsw_ctx** out, int device) {
   if (const char* ev = std::getenv("LSW_FACTOR_TC")) c->factor_tc = std::atoi(ev) != 0;
   // LSW_SHIFT_STREAMS=0 keeps each captured front one launch on one stream
   if (const char* ev = std::getenv("LSW_SHIFT_STREAMS")) c->split_shifts = std::atoi(ev) != 0;
+  // LSW_SWEEP_LANES=<n>: per-sweep launches for batches of at most n right-hand sides (0: never)
+  if (const char* ev = std::getenv("LSW_SWEEP_LANES")) c->lanes_max_rhs = std::max(0, std::atoi(ev));
   // LSW_TUNE=0 leaves every sweep-front shape to the cost model
   if (const char* ev = std::getenv("LSW_TUNE")) c->tune = std::atoi(ev) != 0;
   // LSW_SWEEP_TC=1 adds tensor-core line products to the complex64 tuning candidates
@@ -840,6 +932,20 @@ lsw_status lsw_ctx_set_tuning(lsw_ctx* ctx, int enable) {
     ctx->sched_bufs.clear();
   }
   ctx->tune = enable != 0;
+  return LSW_OK;
+}
+
+lsw_status lsw_ctx_set_sweep_lanes(lsw_ctx* ctx, int max_rhs) {
+  if (!ctx || max_rhs < 0) return fail(ctx, LSW_ERR_INVALID_ARGUMENT, "bad arguments to lsw_ctx_set_sweep_lanes");
+  if (ctx->lanes_max_rhs != max_rhs) {
+    // the schedules built under the other setting are rebuilt on next use
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    CK(cudaDeviceSynchronize(), "sync");
+    ctx->drop_graphs();
+    ctx->sched.clear();
+    ctx->sched_bufs.clear();
+  }
+  ctx->lanes_max_rhs = max_rhs;
   return LSW_OK;
 }
 
@@ -1073,16 +1179,22 @@ lsw_status lsw_apply_precond_profiled(lsw_ctx* ctx, const void* x, void* y, int 
   const double cs = (double)csize(ctx->prec);
   double bytes = 0.0, flops = 0.0, streamed = 0.0;
   int slots = 0;
-  for (const Front& fr : sc->fronts) {
-    std::map<int, int> per_cell;
-    for (int i = fr.item_begin; i < fr.item_begin + fr.item_count; ++i) per_cell[items[i].cell] += items[i].slot_count;
-    for (const auto& kv : per_cell) {
+  // (per-sweep launches of one step count a cell's factor once for the step,
+  // as one launch per step does)
+  std::map<std::pair<int, int>, std::map<int, int>> per_step;
+  for (const Front& fr : sc->fronts)
+    for (int i = fr.item_begin; i < fr.item_begin + fr.item_count; ++i)
+      per_step[{fr.stage, fr.step}][items[i].cell] += items[i].slot_count;
+  for (const auto& st_cells : per_step) {
+    for (const auto& kv : st_cells.second) {
       const DevCell& c = ctx->cells[kv.first];
       const double F = (double)c.nx * c.ny * c.ny * cs;
       bytes += 2.0 * F + 4.0 * kv.second * (double)c.nx * c.ny * cs;
       flops += 2.0 * 8.0 * (double)c.nx * c.ny * c.ny * kv.second;
       slots += kv.second;
     }
+  }
+  for (const Front& fr : sc->fronts) {
     for (int i = fr.item_begin; i < fr.item_begin + fr.item_count; ++i) {
       const DevCell& c = ctx->cells[items[i].cell];
       streamed += 2.0 * (double)c.nx * c.ny * c.ldn * cs + 4.0 * items[i].slot_count * (double)c.nx * c.ny * cs;

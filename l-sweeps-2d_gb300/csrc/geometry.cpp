@@ -95,6 +95,12 @@ Profile1D make_profile(int nel, int p, double h, double C) {
 // one anti-diagonal per front.  The four shifted decompositions of
 // applyPrecond (687-739) and every right-hand side share each front.
 // ---------------------------------------------------------------------------
+// Slots of an item as the sweep kernel instantiates them: at most 8
+// (complex128) or 16, padded to 1, 2, 4, 8, 12 or 16; 8 or 16 on the tensor cores.
+int front_rmax(bool dbl) { return dbl ? 8 : 16; }
+int front_tc_slots(int n) { return n <= 8 ? 8 : 16; }
+int front_rpad(int n) { return n <= 1 ? 1 : n <= 2 ? 2 : n <= 4 ? 4 : n <= 8 ? 8 : n <= 12 ? 12 : 16; }
+
 namespace {
 
 struct SlotSpec {
@@ -293,9 +299,52 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
       emit(parts, count);
     }
   };
+  // ---- launches: one per front, or with plan.lanes one per (front, sweep) ----
+  // fr[0] is stage 1, fr[1 .. N-1] stage 2 (t = 1 .. N-1), fr[N + dd] stage 3
+  // (dd = 0 .. 2N-4); a slot's `order` is its sweep within the stage
+  struct Launch {
+    std::map<int, std::vector<SlotSpec>> cells;
+    int stage = 1, step = 0, lane = -1;
+  };
+  std::vector<Launch> launches;
+  for (size_t q = 0; q < fr.size(); ++q) {
+    const int stage = q == 0 ? 1 : (q < (size_t)N ? 2 : 3);
+    const int step = stage == 1 ? 0 : (stage == 2 ? (int)q : (int)q - N);
+    if (!plan.lanes || stage == 1) {
+      Launch L;
+      L.cells = std::move(fr[q]);
+      L.stage = stage; L.step = step;
+      launches.push_back(std::move(L));
+      continue;
+    }
+    Launch L[4];
+    for (auto& kv : fr[q])
+      for (const SlotSpec& sp : kv.second) L[sp.order].cells[kv.first].push_back(sp);
+    for (int w = 0; w < 4; ++w) {
+      L[w].stage = stage; L[w].step = step; L[w].lane = stage == 2 ? w : 4 + w;
+      launches.push_back(std::move(L[w]));
+    }
+  }
+  const int planes = plan.lanes ? kLanePlanes : 1;
+
   fronts.clear(); items.clear(); slots.clear(); groups.clear();
-  for (size_t fidx = 0; fidx < fr.size(); ++fidx) {
-    auto& f = fr[fidx];
+  for (size_t fidx = 0; fidx < launches.size(); ++fidx) {
+    auto& f = launches[fidx].cells;
+    const int stage = launches[fidx].stage, lane = launches[fidx].lane;
+    // output plane of this launch's groups
+    const int plane = lane < 0 ? 0 : (lane < 4 ? lane : kLanePlane3[lane - 4]);
+    // with per-sweep launches a stage-2 / stage-3 launch shares the GPU with
+    // the other sweeps' launches: the cost model counts it as that many
+    const double conc = (plan.lanes && stage > 1) ? plan.lane_concurrency : 1.0;
+    if (f.empty()) {
+      Front F{(int)items.size(), 0, 0, 0, 1};
+      F.slots_cap = plan.rmax;
+      F.stage = stage; F.step = launches[fidx].step; F.lane = lane;
+      F.mixed = true;
+      for (int sh = 0; sh <= 4; ++sh) F.sh_begin[sh] = 0;
+      fronts.push_back(F);
+      continue;
+    }
     // slots ordered by (shift, rhs): items of 8 or 16 slots merge the groups of
     // one shifted decomposition when there are several right-hand sides, so
     // that the front can run as one launch per shift (see below)
@@ -339,11 +388,12 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
           const int mc = std::max(1, plan.max_clusters[cl]);
           if (plan.max_clusters[cl] <= 0 && cl > 1) continue;
           if (!(plan.fit_mask[R] & (1 << cl))) continue;   // shared memory
-          const long long waves = (n_items + mc - 1) / mc;
+          const long long n_eff = (long long)std::ceil((double)n_items * conc);
+          const long long waves = (n_eff + mc - 1) / mc;
           const double line = plan.line_overhead + plan.slot_cost * R +
                               (plan.col_cost + plan.col_slot_cost * R) * ((ny_max + cl - 1) / cl);
           double t = (double)waves * (2.0 * nf + 1.0) * line;
-          t = std::max(t, fac_elems * plan.csize / plan.bytes_per_cycle);
+          t = std::max(t, conc * fac_elems * plan.csize / plan.bytes_per_cycle);
           // ties go to fewer items (less factor traffic), then to larger clusters
           if (t < best_t * 0.98 || (t <= best_t * 1.02 && n_items < best_items)) {
             best_t = t; best_r = r; best_cl = cl; best_items = n_items;
@@ -359,6 +409,7 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
     if (best_t >= 1e300) throw std::runtime_error("no sweep-front launch shape fits in shared memory");
     Front F{(int)items.size(), 0, 0, 0, best_cl};
     F.slots_cap = best_r;
+    F.stage = stage; F.step = launches[fidx].step; F.lane = lane;
     for (auto& kv : f) {
       const int c = kv.first;
       auto& v = kv.second;
@@ -373,7 +424,7 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
           g.slot_begin = (int)slots.size() - it.slot_begin;
           g.slot_count = int(pr.second - pr.first);
           g.shift = v[pr.first].shift;
-          g.out_off = ((long long)v[pr.first].rhs * 4 + v[pr.first].shift) * n_dof2;
+          g.out_off = (((long long)v[pr.first].rhs * planes + plane) * 4 + v[pr.first].shift) * n_dof2;
           groups.push_back(g);
           for (size_t q = pr.first; q < pr.second; ++q) slots.push_back(v[q].s);
           it.group_count++;
@@ -399,7 +450,8 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
         return sh;
       };
       auto first = items.begin() + F.item_begin;
-      F.mixed = false;
+      // per-sweep launches run on their own streams instead: one launch each
+      F.mixed = plan.lanes;
       for (auto it = first; it != items.end(); ++it)
         if (item_shift(*it) < 0) F.mixed = true;
       if (!F.mixed)
@@ -421,8 +473,17 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
   // sized for its largest front.  A mixed front runs alone (every shift's
   // stream joined) and lays its items out from 0.  Every front records the
   // pool size in scratch_elems.
-  long long region[4] = {0, 0, 0, 0}, mixed_max = 0;
+  // With per-sweep launches each sweep's chain of launches has its own region
+  // (sized for its largest launch) and stage 1, which runs alone, is laid out
+  // from 0.
+  long long region[4] = {0, 0, 0, 0}, mixed_max = 0, lane_region[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   for (const Front& F : fronts) {
+    if (F.lane >= 0) {
+      long long t = 0;
+      for (int i = F.item_begin; i < F.item_begin + F.item_count; ++i) t += items[i].scratch_off;
+      lane_region[F.lane] = std::max(lane_region[F.lane], t);
+      continue;
+    }
     if (F.mixed) {
       long long t = 0;
       for (int i = F.item_begin; i < F.item_begin + F.item_count; ++i) t += items[i].scratch_off;
@@ -436,9 +497,18 @@ void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const Fr
     }
   }
   const long long base[4] = {0, region[0], region[0] + region[1], region[0] + region[1] + region[2]};
-  const long long pool = std::max(base[3] + region[3], mixed_max);
+  long long lane_base[8], lane_total = 0;
+  for (int l = 0; l < 8; ++l) { lane_base[l] = lane_total; lane_total += lane_region[l]; }
+  const long long pool = std::max(std::max(base[3] + region[3], mixed_max), lane_total);
   for (Front& F : fronts) {
-    if (F.mixed) {
+    if (F.lane >= 0) {
+      long long off = lane_base[F.lane];
+      for (int i = F.item_begin; i < F.item_begin + F.item_count; ++i) {
+        const long long sz = items[i].scratch_off;
+        items[i].scratch_off = off;
+        off += sz;
+      }
+    } else if (F.mixed) {
       long long off = 0;
       for (int i = F.item_begin; i < F.item_begin + F.item_count; ++i) {
         const long long sz = items[i].scratch_off;

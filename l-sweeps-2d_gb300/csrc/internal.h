@@ -99,7 +99,27 @@ struct Front {
   bool tc = false;        // complex64 line products on the tensor cores
   bool mixed = false;     // an item mixes shifted decompositions: the front is one launch
   int sh_begin[5] = {0, 0, 0, 0, 0};   // items of shift s: [sh_begin[s], sh_begin[s + 1]) (not mixed)
+  // the sweep step this launch belongs to: stage (1, 2, 3) and step (stage 2:
+  // column / row t = 1..N-1; stage 3: anti-diagonal 0..2N-4); with per-sweep
+  // launches, the sweep (lane): stage 2 right, left, up, down = 0..3, stage 3
+  // BL2TR, TR2BL, BR2TL, TL2BR = 4..7; -1 when the launch holds every sweep
+  int stage = 1, step = 0, lane = -1;
 };
+
+// Per-sweep launches.  The four stage-2 sweeps of DDCheckerboard::applySweep
+// read and write disjoint trace lines, and so do the four L-sweeps of stage
+// 3; an L-sweep's step dd reads only traces that stage 1, its own earlier
+// steps and two stage-2 sweeps (its producers) wrote, the latter by their
+// front min(dd + 1, N - 1).  With one launch per (step, sweep), each sweep
+// runs as its own chain and the L-sweeps start while stage 2 still runs.
+// Outputs: one plane per stage-2 sweep (per right-hand side and shift); an
+// L-sweep adds into the plane of one of its producers, whose writes to any
+// cell it reaches are ordered before it by that wait.
+constexpr int kLanePlanes = 4;
+// stage-3 lane w (0..3): its two producing stage-2 sweeps and its output plane
+constexpr int kLaneProducerLR[4] = {2, 3, 2, 3};   // up, down, up, down (TS_LRUP / TS_LRDOWN)
+constexpr int kLaneProducerUD[4] = {0, 1, 1, 0};   // right, left, left, right (TS_UDRIGHT / TS_UDLEFT)
+constexpr int kLanePlane3[4] = {2, 3, 1, 0};       // BL2TR->up, TR2BL->down, BR2TL->left, TL2BR->right
 
 // What the front planner knows about the device: how many clusters of each
 // size (1, 2, 4, 8) are resident at once, and a per-line cost model of the
@@ -126,10 +146,16 @@ struct FrontPlan {
   // items may run with tensor-core line products (8 or 16 slots, fewer
   // padded): their forward storage is sized for that many slots
   bool tc_scratch = false;
+  // one launch per (step, sweep) instead of one per step (see kLanePlanes);
+  // the cost model then counts a stage-2 / stage-3 launch as sharing the GPU
+  // with `lane_concurrency` others of its size
+  bool lanes = false;
+  double lane_concurrency = 4.0;
 };
 
 struct Schedule {
   int nrhs = 0;
+  bool lanes = false;     // per-sweep launches, kLanePlanes output planes
   std::vector<Front> fronts;
   DevItem* d_items = nullptr;
   DevSlot* d_slots = nullptr;
@@ -139,7 +165,11 @@ struct Schedule {
 };
 
 // Build the sweep schedule (stage 1, N-1 stage-2 fronts, 2N-3 stage-3 fronts,
-// all four shifted decompositions and nrhs right-hand sides in every front).
+// all four shifted decompositions and nrhs right-hand sides in every front;
+// with plan.lanes every stage-2 / stage-3 front is split into one launch per
+// sweep, in the order stage 1, stage 2 (t, then sweep), stage 3 (dd, then sweep)).
+// Output groups address the out pool as [rhs][plane][shift] n_dof2 with one
+// plane, or kLanePlanes planes with plan.lanes.
 void build_schedule(const std::vector<DevCell>& cells, int N, int nrhs, const FrontPlan& plan, long long LP,
                     std::vector<Front>& fronts, std::vector<DevItem>& items, std::vector<DevSlot>& slots,
                     std::vector<DevGroup>& groups, long long n_dof2);
@@ -225,9 +255,10 @@ template <typename T> cudaError_t launch_combine(const void* outs, double2* y, i
                                                  cudaStream_t st);
 cudaError_t launch_rhs(double2* b, int n_dof, int p, double h, const double* src, const double* amp,
                        int nsrc, double eps, cudaStream_t st);
-// combine into *y_ref (the output address read from device memory)
+// combine into *y_ref (the output address read from device memory); the out
+// pool holds `planes` planes of the four shifted outputs per right-hand side
 template <typename T> cudaError_t launch_combine_ref(const void* outs, double2* const* y_ref, int nrhs, long long n2,
-                                                     cudaStream_t st);
+                                                     int planes, cudaStream_t st);
 // ref[0] = x, ref[1] = y (the address table of a captured apply)
 cudaError_t launch_set_refs(const void** ref, const void* x, void* y, cudaStream_t st);
 

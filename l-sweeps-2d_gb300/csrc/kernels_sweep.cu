@@ -1159,9 +1159,6 @@ size_t smem_need(int ldn_max, int ny_max, int nx_max, int R, int KSW, int CL, in
 
 }  // namespace
 
-int front_rmax(bool dbl) { return dbl ? 8 : 16; }
-int front_tc_slots(int n) { return n <= 8 ? 8 : 16; }
-int front_rpad(int n) { return n <= 1 ? 1 : n <= 2 ? 2 : n <= 4 ? 4 : n <= 8 ? 8 : n <= 12 ? 12 : 16; }
 
 namespace {
 

@@ -223,16 +223,23 @@ template cudaError_t launch_combine<double>(const void*, double2*, int, long lon
 
 namespace {
 template <typename T>
-__global__ void k_combine_ref(const cx_t<T>* __restrict__ o, double2* const* __restrict__ yref, long long n2) {
+__global__ void k_combine_ref(const cx_t<T>* __restrict__ o, double2* const* __restrict__ yref, long long n2,
+                              int planes) {
   const long long G = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int v = blockIdx.y;
   if (G >= n2) return;
   double2* y = *yref;
-  const cx_t<T>* b = o + (long long)v * 4 * n2;
   const double2 z = make_double2(0, 0);
-  const double2 a0 = to_c(b[G], z), a1 = to_c(b[n2 + G], z), a2 = to_c(b[2 * n2 + G], z),
-                a3 = to_c(b[3 * n2 + G], z);
-  y[(long long)v * n2 + G] = cadd(a0, cadd(cadd(a1, a2), a3));
+  // per plane the four shifted outputs, a0 + ((a1 + a2) + a3); the planes in order
+  double2 acc = z;
+  for (int l = 0; l < planes; ++l) {
+    const cx_t<T>* b = o + ((long long)v * planes + l) * 4 * n2;
+    const double2 a0 = to_c(b[G], z), a1 = to_c(b[n2 + G], z), a2 = to_c(b[2 * n2 + G], z),
+                  a3 = to_c(b[3 * n2 + G], z);
+    const double2 s = cadd(a0, cadd(cadd(a1, a2), a3));
+    acc = l == 0 ? s : cadd(acc, s);
+  }
+  y[(long long)v * n2 + G] = acc;
 }
 __global__ void k_set_refs(const void** ref, const void* x, void* y) {
   ref[0] = x;
@@ -241,13 +248,14 @@ __global__ void k_set_refs(const void** ref, const void* x, void* y) {
 }  // namespace
 
 template <typename T>
-cudaError_t launch_combine_ref(const void* outs, double2* const* y_ref, int nrhs, long long n2, cudaStream_t st) {
+cudaError_t launch_combine_ref(const void* outs, double2* const* y_ref, int nrhs, long long n2, int planes,
+                               cudaStream_t st) {
   dim3 g((unsigned)((n2 + kVT - 1) / kVT), (unsigned)nrhs);
-  k_combine_ref<T><<<g, kVT, 0, st>>>(reinterpret_cast<const cx_t<T>*>(outs), y_ref, n2);
+  k_combine_ref<T><<<g, kVT, 0, st>>>(reinterpret_cast<const cx_t<T>*>(outs), y_ref, n2, planes);
   return cudaGetLastError();
 }
-template cudaError_t launch_combine_ref<float>(const void*, double2* const*, int, long long, cudaStream_t);
-template cudaError_t launch_combine_ref<double>(const void*, double2* const*, int, long long, cudaStream_t);
+template cudaError_t launch_combine_ref<float>(const void*, double2* const*, int, long long, int, cudaStream_t);
+template cudaError_t launch_combine_ref<double>(const void*, double2* const*, int, long long, int, cudaStream_t);
 
 cudaError_t launch_set_refs(const void** ref, const void* x, void* y, cudaStream_t st) {
   k_set_refs<<<1, 1, 0, st>>>(ref, x, y);

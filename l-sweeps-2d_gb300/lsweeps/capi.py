@@ -23,7 +23,7 @@ EXPORTS = [
     "lsw_apply_A", "lsw_assemble_rhs", "lsw_gmres", "lsw_solve_host", "lsw_local_solve",
     "lsw_apply_precond_profiled", "lsw_local_solve_noalloc", "lsw_release_workspace",
     "lsw_ctx_set_wait_limit", "lsw_selftest_bounded_wait", "lsw_ctx_set_graphs", "lsw_ctx_set_tuning",
-    "lsw_front_shapes",
+    "lsw_ctx_set_sweep_lanes", "lsw_front_shapes",
 ]
 
 
@@ -114,6 +114,7 @@ def lib() -> C.CDLL:
         "lsw_selftest_bounded_wait": (i, [vp, vp]),
         "lsw_ctx_set_graphs": (i, [vp, i]),
         "lsw_ctx_set_tuning": (i, [vp, i]),
+        "lsw_ctx_set_sweep_lanes": (i, [vp, i]),
         "lsw_front_shapes": (i, [vp, i, C.POINTER(FrontShape), i, C.POINTER(i), C.POINTER(d), vp]),
     }
     for name, (res, args) in sig.items():

@@ -104,7 +104,7 @@ class Solver:
         (lsw_front_shapes) and the context's tuning time in seconds."""
         n = C.c_int(0)
         ts = C.c_double(0.0)
-        cap = 4 * self.spec.N + 8
+        cap = 16 * self.spec.N + 16   # one launch per step, or per (step, sweep) for small batches
         buf = (capi.FrontShape * cap)()
         capi.check(self.L.lsw_front_shapes(self.ctx, nrhs, buf, cap, C.byref(n), C.byref(ts), _stream_ptr(stream)),
                    self.ctx)
@@ -113,6 +113,11 @@ class Solver:
     def set_tuning(self, enable: bool):
         """Measure sweep-front shapes on first use (lsw_ctx_set_tuning)."""
         capi.check(self.L.lsw_ctx_set_tuning(self.ctx, 1 if enable else 0), self.ctx)
+
+    def set_sweep_lanes(self, max_rhs: int):
+        """Per-sweep launches for batches of at most max_rhs right-hand sides
+        (lsw_ctx_set_sweep_lanes; 0 turns them off)."""
+        capi.check(self.L.lsw_ctx_set_sweep_lanes(self.ctx, int(max_rhs)), self.ctx)
 
     def set_graphs(self, enable: bool):
         """Replay applies as CUDA graphs (lsw_ctx_set_graphs)."""

@@ -1,7 +1,8 @@
-"""Sweep-front autotuner: the first apply of a batch size measures every
-launch shape (slots per item x CTAs per half chain) on every front and keeps
-the fastest; the choice is cached per GPU and problem shape in the process
-and, with LSW_TUNE_CACHE, in a file that a later process reads back.
+"""Sweep-front autotuner: the first apply of a batch size that runs one
+launch per sweep step measures every launch shape (slots per item x CTAs per
+half chain) on every front and keeps the fastest; the choice is cached per
+GPU and problem shape in the process and, with LSW_TUNE_CACHE, in a file that
+a later process reads back.
 
 Shapes change only how the cells' right-hand sides are grouped into launches
 and how a cell's columns are split over CTAs, so tuned and cost-model
@@ -39,8 +40,11 @@ def rel(a, b):
 
 
 @pytest.mark.parametrize("prec,tol", [("c128", 1e-10), ("c64", 2e-4), ("bf16x2", 2e-4)])
-def test_tuned_schedule_matches_model_and_oracle(prec, tol):
+def test_tuned_schedule_matches_model_and_oracle(prec, tol, monkeypatch):
     from lsweeps.solver import Solver
+    # single vectors run one launch per step here: per-sweep launches (the
+    # default for one right-hand side) take their shapes from the cost model
+    monkeypatch.setenv("LSW_SWEEP_LANES", "0")
     spec, d = _load(FIXTURES[-1])
     v = torch.from_numpy(d["v"]).cuda()
     S0 = Solver(spec, d["m_grid"], precision=prec)
