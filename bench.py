@@ -404,11 +404,17 @@ def run_gpu(args):
     # DRAM traffic of the fronts: the ncu capture's traffic per algorithmic
     # byte (a full C2 apply of the same kernel and precision) times this
     # apply's algorithmic bytes
-    traffic = None
+    # (the capture of the same schedule kind: per-sweep launches or one launch
+    # per step, where one exists)
+    traffic, traffic_key = None, None
     tf = ROOT / "profiles" / "k_front_dram_traffic.md"
     if tf.exists() and prec in ("c64", "bf16x2"):
-        m = re.search(r"traffic_per_alg_byte_%s:\s*([0-9.eE+]+)" % prec, tf.read_text())
-        traffic = float(m.group(1)) * pr["alg_bytes"] if m else None
+        keys = ([prec + "_per_sweep"] if launch["per_sweep_launches"] else []) + [prec]
+        for key in keys:
+            m = re.search(r"traffic_per_alg_byte_%s:\s*([0-9.eE+]+)" % key, tf.read_text())
+            if m:
+                traffic, traffic_key = float(m.group(1)) * pr["alg_bytes"], key
+                break
 
     # plain FP64 GPU path
     S64 = None
@@ -470,8 +476,8 @@ def run_gpu(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak if peak else None, "traffic": traffic,
                          "traffic_source": "ncu DRAM bytes per algorithmic byte of a full C2 apply of this kernel "
-                                           "and precision (profiles/k_front_dram_traffic.md), times this apply's "
-                                           "algorithmic bytes" if traffic else None,
+                                           "(traffic_per_alg_byte_%s in profiles/k_front_dram_traffic.md), times "
+                                           "this apply's algorithmic bytes" % traffic_key if traffic else None,
                          "kernel": "k_front (sweep-front cell solves), all fronts of one apply (graph replay)",
                          "achieved_fronts_one_by_one": achieved_sequential,
                          "peak_kind": peak_kind, "alg_bytes_per_apply": pr["alg_bytes"],

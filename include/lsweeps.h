@@ -191,9 +191,12 @@ lsw_status lsw_ctx_set_tuning(lsw_ctx* ctx, int enable);
  * to one plane per stage-2 sweep, summed at the end (four times the output
  * pool of one launch per step).  Results equal those of one launch per step up
  * to the order of the final sums.  Their launch shapes come from the cost
- * model (launches timed alone do not show how they share the GPU).  Changing
- * the setting drops the context's schedules (rebuilt on next use; waits for
- * the device).  No counterpart in the reference (its sweeps are host loops,
+ * model, with each launch assumed to share the GPU with 2, 4 or 8 others of
+ * its size (launches timed alone do not show that sharing): with tuning on
+ * (lsw_ctx_set_tuning) the first apply of a batch size times one whole apply
+ * per assumption and keeps the fastest, cached like the per-front shapes;
+ * with tuning off the assumption is 4.  Changing the setting drops the
+ * context's schedules (rebuilt on next use; waits for the device).  No counterpart in the reference (its sweeps are host loops,
  * DDCheckerboard.cpp:812-880). */
 lsw_status lsw_ctx_set_sweep_lanes(lsw_ctx* ctx, int max_rhs);
 

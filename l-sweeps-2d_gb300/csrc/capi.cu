@@ -276,6 +276,8 @@ lsw_status ensure_pools(lsw_ctx* ctx, int nrhs, long long scratch_elems, int pla
 }
 
 lsw_status launch_front_of(lsw_ctx* ctx, const Schedule* sc, size_t fi, cudaStream_t st, int i0 = 0, int i1 = -1);
+lsw_status enqueue_apply(lsw_ctx* ctx, Schedule* sc, int nrhs, cudaStream_t st, int* kernels,
+                         bool split_shifts = false);
 lsw_status check_kernel_err(lsw_ctx* ctx, cudaStream_t st);
 
 // ---- sweep-front autotuner ----
@@ -429,6 +431,64 @@ lsw_status tune_fronts(lsw_ctx* ctx, int nrhs, const FrontPlan& plan, cudaStream
   return s;
 }
 
+// Per-sweep schedules are tuned as a whole: their launches share the GPU with
+// one another, which a launch timed alone does not show.  For each candidate
+// of the cost model's concurrency (how many launches of its size a per-sweep
+// launch is assumed to share the GPU with: 2, 4, 8) the schedule is built and
+// one whole apply (eager launches on the sweep streams, a zero vector) is
+// timed with CUDA events on the caller's stream after one untimed apply; the
+// entry keeps each candidate's time (r = the candidate, ms = its apply).
+lsw_status tune_lanes(lsw_ctx* ctx, int nrhs, const FrontPlan& plan, cudaStream_t st, TuneEntry* out) {
+  const auto t_start = std::chrono::steady_clock::now();
+  DevBuf tx, ty;
+  CK(tx.ensure((size_t)nrhs * ctx->n2 * sizeof(double2)), "cudaMalloc(tuning vector)");
+  CK(ty.ensure((size_t)nrhs * ctx->n2 * sizeof(double2)), "cudaMalloc(tuning vector)");
+  CK(cudaMemsetAsync(tx.p, 0, tx.bytes, st), "memset tuning vector");
+  CK(ctx->d_ref.ensure(2 * sizeof(void*)), "cudaMalloc(address table)");
+  KL(1, launch_set_refs(reinterpret_cast<const void**>(ctx->d_ref.p), tx.p, ty.p, st), "address table");
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CK(cudaEventCreate(&e0), "cudaEventCreate");
+  CK(cudaEventCreate(&e1), "cudaEventCreate");
+  lsw_status s = LSW_OK;
+  bool warm = false;
+  for (int conc : {2, 4, 8}) {
+    FrontPlan p = plan;
+    p.lane_concurrency = conc;
+    Schedule sc;
+    sc.lanes = true;
+    sc.nrhs = nrhs;
+    DevBuf bufs[3];
+    std::vector<DevItem> items; std::vector<DevSlot> slots; std::vector<DevGroup> groups;
+    try {
+      build_schedule(ctx->cells, ctx->N, nrhs, p, ctx->LP, sc.fronts, items, slots, groups, ctx->n2);
+    } catch (const std::exception&) {
+      continue;
+    }
+    if ((s = upload_schedule(ctx, &sc, items, slots, groups, bufs)) != LSW_OK) break;
+    if ((s = ensure_pools(ctx, nrhs, sc.scratch_elems, kLanePlanes)) != LSW_OK) break;
+    float ms = 0.f;
+    for (int rep = warm ? 1 : 0; rep < 2 && s == LSW_OK; ++rep) {
+      int k = 0;
+      if (cudaEventRecord(e0, st) != cudaSuccess) { s = fail(ctx, LSW_ERR_CUDA, "event"); break; }
+      if ((s = enqueue_apply(ctx, &sc, nrhs, st, &k)) != LSW_OK) break;
+      ctx->launches += k;
+      if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+          cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+        s = fail(ctx, LSW_ERR_CUDA, "timing a per-sweep schedule");
+    }
+    warm = true;
+    if (s == LSW_OK) s = check_kernel_err(ctx, st);
+    if (s != LSW_OK) break;
+    out->r.push_back(conc); out->cl.push_back(0); out->tc.push_back(0); out->ms.push_back(ms);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CK(cudaStreamSynchronize(st), "tuning sync");
+  ctx->d_scratch.release();
+  ctx->tune_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  return s;
+}
+
 lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out, cudaStream_t st) {
   auto it = ctx->sched.find(nrhs);
   void* const before[3] = {ctx->d_traces.p, ctx->d_outs.p, ctx->d_scratch.p};
@@ -446,9 +506,27 @@ lsw_status ensure_batch(lsw_ctx* ctx, int nrhs, Schedule** out, cudaStream_t st)
     if (ctx->force_r > 0) {
       plan.forced_r.assign(16 * (size_t)ctx->N + 16, ctx->force_r);
       plan.forced_cl.assign(16 * (size_t)ctx->N + 16, ctx->force_cl);
-    } else if (ctx->tune && ctx->factorized && !plan.lanes) {
-      // (per-sweep launches run concurrently with one another, which a launch
-      // timed alone does not show: their shapes come from the cost model)
+    } else if (ctx->tune && ctx->factorized && plan.lanes) {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      tune_file_read();
+      const std::string key = tune_key(ctx, nrhs) + "|lanes";
+      auto hit = g_tune_cache.find(key);
+      TuneEntry whole;
+      if (hit != g_tune_cache.end()) {
+        whole = hit->second;
+      } else {
+        lsw_status s = tune_lanes(ctx, nrhs, plan, st, &whole);
+        if (s != LSW_OK) return s;
+        if (!whole.r.empty()) {
+          g_tune_cache[key] = whole;
+          tune_file_append(key, whole);
+        }
+      }
+      size_t best = 0;
+      for (size_t i = 1; i < whole.ms.size(); ++i)
+        if (whole.ms[i] < whole.ms[best]) best = i;
+      if (!whole.r.empty()) plan.lane_concurrency = whole.r[best];
+    } else if (ctx->tune && ctx->factorized) {
       std::lock_guard<std::mutex> lk(g_tune_mu);
       tune_file_read();
       const std::string key = tune_key(ctx, nrhs);
@@ -611,7 +689,7 @@ lsw_status enqueue_lanes(lsw_ctx* ctx, Schedule* sc, cudaStream_t st, int* k, bo
 // Per-sweep schedules (sc->lanes) run on the sweep streams of enqueue_lanes,
 // captured or not (one stream when the fronts are timed one by one).
 lsw_status enqueue_apply(lsw_ctx* ctx, Schedule* sc, int nrhs, cudaStream_t st, int* kernels,
-                         bool split_shifts = false) {
+                         bool split_shifts) {
   const size_t cs = csize(ctx->prec);
   const int planes = sc->lanes ? kLanePlanes : 1;
   CK(cudaMemsetAsync(ctx->d_traces.p, 0, (size_t)nrhs * 4 * ctx->ncell * 24 * ctx->LP * cs, st), "memset traces");

@@ -89,3 +89,31 @@ def test_per_sweep_solve_matches_one_launch_per_step(monkeypatch):
     assert r0.converged and r1.converged and r1.true_rel_res <= 1e-8
     assert abs(r1.iterations - r0.iterations) <= 1
     assert rel(x1, x0) <= 1e-6
+
+
+def test_per_sweep_schedule_is_tuned_as_a_whole(monkeypatch):
+    """With tuning on, the first single-vector apply times one whole apply per
+    assumed sharing of the GPU (2, 4, 8 launches) and keeps the fastest; a
+    second context in the process reads the choice from the cache (measures
+    nothing) and builds the same launches, and the tuned applies match the
+    oracle.  (A cluster cap of 4 CTAs per cell solve gives this test a problem
+    shape of its own in the process-wide cache.)"""
+    from lsweeps.solver import Solver
+    monkeypatch.setenv("LSW_MAX_CLUSTER", "4")
+    spec, d = _load(FIXTURES[-1])
+    v = torch.from_numpy(d["v"]).cuda()
+    runs = []
+    for _ in range(2):
+        S = Solver(spec, d["m_grid"], precision="c64")
+        S.factorize()
+        shapes, tune_s = S.front_shapes(1)
+        y = S.apply_precond(v).cpu().numpy()
+        runs.append((shapes, tune_s, y))
+        S.close()
+    (sh1, t1, y1), (sh2, t2, y2) = runs
+    assert t1 > 0.0 and t2 == 0.0
+    key = lambda sh: [(f["items"], f["max_slots"], f["slots_cap"], f["cluster"]) for f in sh]
+    assert key(sh1) == key(sh2)
+    assert all(f["cluster"] <= 2 for f in sh1)      # 2 x cluster CTAs per cell solve, capped at 4
+    assert np.array_equal(y1, y2)
+    assert rel(y1, d["Mv"]) <= 2e-4
