@@ -479,10 +479,13 @@ def run_gpu(args):
                                            "(traffic_per_alg_byte_%s in profiles/k_front_dram_traffic.md), times "
                                            "this apply's algorithmic bytes" % traffic_key if traffic else None,
                          "kernel": "k_front (sweep-front cell solves), all fronts of one apply (graph replay)",
-                         "achieved_fronts_one_by_one": achieved_sequential,
+                         # the launches one by one on one stream (profiled): no overlap between
+                         # launches, so below the replayed apply, far below with per-sweep launches
+                         "achieved_launches_serialised": achieved_sequential,
                          "peak_kind": peak_kind, "alg_bytes_per_apply": pr["alg_bytes"],
                          "streamed_bytes_per_apply": pr["streamed_bytes"],
-                         "front_ms_per_apply": front_ms, "fronts": pr["fronts"], "items": pr["items"],
+                         "launch_ms_per_apply_serialised": front_ms, "launches": pr["fronts"],
+                         "items": pr["items"],
                          "slots": pr["slots"], "apply_ms": pr["total_ms"]},
             "launch_shapes": launch,
             "cpu_baseline": cpu,
