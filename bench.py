@@ -375,15 +375,15 @@ def run_gpu(args):
     model_shapes, _ = S.front_shapes(nrhs)
     S.set_tuning(True)
     apply_ms(1)
-    # with per-sweep launches (a single right-hand side): the apply with one
-    # launch per sweep step beside it, on the same context
+    # with per-sweep launches (batches of one or two right-hand sides): the
+    # apply with one launch per sweep step beside it, on the same context
     steps_per_apply = 3 * spec.N - 3
     t_step_graph = None
     if len(shapes) > steps_per_apply:
         S.set_sweep_lanes(0)
         S.front_shapes(nrhs)
         t_step_graph = apply_ms()
-        S.set_sweep_lanes(nrhs)
+        S.set_sweep_lanes(sweep_lanes_default())
         apply_ms(1)
     launch = {
         "apply_ms_tuned_graph": t_tuned_graph, "apply_ms_tuned_eager": t_tuned_eager,
@@ -547,12 +547,17 @@ def run_apply_only(args):
                 torch.cuda.synchronize()
                 t1.append(e0.elapsed_time(e1))
             line["apply_ms_one_launch_per_step"] = round(statistics.median(t1), 3)
-            S.set_sweep_lanes(args.nrhs)
+            S.set_sweep_lanes(sweep_lanes_default())
     if args.warmup + args.steps > 0:
         # the algorithmic and streamed bytes of one apply (one more, profiled, apply)
         _, pr = S.apply_precond_profiled(v)
         line.update({k: pr[k] for k in ("alg_bytes", "streamed_bytes", "front_ms", "fronts", "items")})
     print(json.dumps(line))
+
+
+def sweep_lanes_default() -> int:
+    """The context's per-sweep launch threshold as created (LSW_SWEEP_LANES or 2)."""
+    return max(0, int(os.environ.get("LSW_SWEEP_LANES", "2")))
 
 
 def run_serve(args):

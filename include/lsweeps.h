@@ -181,7 +181,7 @@ lsw_status lsw_ctx_set_graphs(lsw_ctx* ctx, int enable);
  * reference (its sweeps are host loops, DDCheckerboard.cpp:812-880). */
 lsw_status lsw_ctx_set_tuning(lsw_ctx* ctx, int enable);
 
-/* Per-sweep launches for batches of at most `max_rhs` right-hand sides (1,
+/* Per-sweep launches for batches of at most `max_rhs` right-hand sides (2,
  * the default; LSW_SWEEP_LANES=<n> in the environment at context creation
  * sets it; 0 turns them off).  Such a batch runs every stage-2 sweep and every
  * L-sweep of the preconditioner as its own chain of launches on its own

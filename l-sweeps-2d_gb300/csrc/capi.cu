@@ -92,7 +92,7 @@ struct lsw_ctx {
   // batches of at most this many right-hand sides run every stage-2 and
   // stage-3 sweep as its own chain of launches (one stream per sweep, created
   // on first use; events per stage-2 launch for the L-sweeps' waits)
-  int lanes_max_rhs = 1;
+  int lanes_max_rhs = 2;
   cudaStream_t lane_st[8] = {};
   cudaEvent_t lane_fork = nullptr;
   cudaEvent_t lane_join[8] = {};

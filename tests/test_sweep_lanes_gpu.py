@@ -1,4 +1,4 @@
-"""Per-sweep launches (the schedule of a single right-hand side): every
+"""Per-sweep launches (the schedule of one or two right-hand sides): every
 stage-2 sweep and every L-sweep runs as its own chain of launches on its own
 stream, the L-sweeps starting while stage 2 still runs, with one output plane
 per stage-2 sweep summed at the end.
