@@ -86,6 +86,67 @@ static std::map<std::tuple<int, int, int>, std::multiset<SlotKey>> solves(const 
   return out;
 }
 
+// A launch (or the part of one front launched on one stream): items [i0, i1)
+// of front `front`, after the units in `pred`.
+struct Unit {
+  int front, i0, i1;
+  std::vector<int> pred;
+};
+
+// Every two units that touch the same trace line, output region or scratch
+// range, one of them writing, must be ordered (one an ancestor of the other).
+template <typename Report>
+static void check_races(const Built& b, const std::vector<DevCell>& cells, const std::vector<Unit>& units,
+                        Report& report) {
+  const int L = (int)units.size();
+  std::vector<std::vector<char>> anc(L, std::vector<char>(L, 0));
+  for (int i = 0; i < L; ++i)
+    for (int q : units[i].pred) {
+      if (q >= i) report("edge against the launch order", q, i, 0);
+      anc[i][q] = 1;
+      for (int k = 0; k < L; ++k)
+        if (anc[q][k]) anc[i][k] = 1;
+    }
+  auto ordered = [&](int x, int y) { return x == y || anc[x][y] || anc[y][x]; };
+  // accesses: (unit, write?) per trace line, output region and scratch element range
+  std::map<long long, std::vector<std::pair<int, bool>>> trace, outreg;
+  std::vector<std::tuple<long long, long long, int>> scratch;
+  for (int i = 0; i < L; ++i) {
+    for (int j = units[i].i0; j < units[i].i1; ++j) {
+      const DevItem& it = b.items[j];
+      const DevCell& c = cells[it.cell];
+      for (int q = 0; q < it.slot_count; ++q) {
+        const DevSlot& s = b.slots[it.slot_begin + q];
+        for (long long r : {s.in_lr0, s.in_lr1, s.in_ud0, s.in_ud1})
+          if (r >= 0) trace[r].push_back({i, false});
+        for (int l = 0; l < s.n_lr; ++l) trace[s.lr_out[l]].push_back({i, true});
+        for (int l = 0; l < s.n_ud; ++l) trace[s.ud_out[l]].push_back({i, true});
+      }
+      for (int g = 0; g < it.group_count; ++g) {
+        const DevGroup& G = b.groups[it.group_begin + g];
+        if (G.out_off >= 0) outreg[G.out_off + it.cell].push_back({i, true});   // owned sets of cells are disjoint
+      }
+      const long long len = (long long)(c.nx + 1) * front_rpad(it.slot_count) * c.ny;
+      scratch.emplace_back(it.scratch_off, it.scratch_off + len, i);
+    }
+  }
+  for (auto* acc : {&trace, &outreg})
+    for (const auto& kv : *acc) {
+      const auto& v = kv.second;
+      for (size_t x = 0; x < v.size(); ++x)
+        for (size_t y = x + 1; y < v.size(); ++y)
+          if ((v[x].second || v[y].second) && !ordered(v[x].first, v[y].first))
+            report(acc == &trace ? "unordered trace-line access" : "unordered output write", units[v[x].first].front,
+                   units[v[y].first].front, kv.first);
+    }
+  std::sort(scratch.begin(), scratch.end());
+  for (size_t x = 0; x < scratch.size(); ++x)
+    for (size_t y = x + 1; y < scratch.size() && std::get<0>(scratch[y]) < std::get<1>(scratch[x]); ++y)
+      if (!ordered(std::get<2>(scratch[x]), std::get<2>(scratch[y])))
+        report("unordered scratch overlap", units[std::get<2>(scratch[x])].front,
+               units[std::get<2>(scratch[y])].front, std::get<0>(scratch[y]));
+}
+
 int main(int argc, char** argv) {
   if (argc != 5) {
     std::fprintf(stderr, "usage: schedule_probe N m p nrhs\n");
@@ -125,84 +186,86 @@ int main(int argc, char** argv) {
     }
   }
 
-  // 3. the launch order and the races it allows
-  const int L = (int)per.fronts.size();
-  std::vector<std::vector<int>> pred(L);
-  int last_stage1 = -1;
-  bool forked = false;
-  std::vector<int> last_of_lane(8, -1);
-  std::map<std::pair<int, int>, int> stage2_launch;   // (sweep, t) -> launch
-  for (int i = 0; i < L; ++i) {
-    const Front& f = per.fronts[i];
-    if (f.lane < 0) {
-      if (last_stage1 >= 0) pred[i].push_back(last_stage1);
-      if (forked || f.stage != 1) report("launch on the main stream after the fork", i, -1, f.stage);
-      last_stage1 = i;
-      continue;
-    }
-    forked = true;
-    const int prev = last_of_lane[f.lane] >= 0 ? last_of_lane[f.lane] : last_stage1;
-    if (prev >= 0) pred[i].push_back(prev);
-    if (f.stage == 2) stage2_launch[{f.lane, f.step}] = i;
-    if (f.stage == 3) {
-      const int w = f.lane - 4, t = std::min(f.step + 1, N - 1);
-      for (int src : {kLaneProducerLR[w], kLaneProducerUD[w]}) {
-        auto it = stage2_launch.find({src, t});
-        if (it == stage2_launch.end()) report("missing producer launch", i, src, t);
-        else pred[i].push_back(it->second);
+  // 3. the per-sweep launches as the library orders them, and the races that
+  // order allows
+  std::vector<Unit> units;
+  {
+    int last_stage1 = -1;
+    bool forked = false;
+    std::vector<int> last_of_lane(8, -1);
+    std::map<std::pair<int, int>, int> stage2_launch;   // (sweep, t) -> unit
+    for (int i = 0; i < (int)per.fronts.size(); ++i) {
+      const Front& f = per.fronts[i];
+      Unit u{i, f.item_begin, f.item_begin + f.item_count, {}};
+      const int id = (int)units.size();
+      if (f.lane < 0) {
+        if (last_stage1 >= 0) u.pred.push_back(last_stage1);
+        if (forked || f.stage != 1) report("launch on the main stream after the fork", i, -1, f.stage);
+        last_stage1 = id;
+        units.push_back(u);
+        continue;
       }
-    }
-    last_of_lane[f.lane] = i;
-  }
-  // ancestors (every edge goes from an earlier to a later launch)
-  std::vector<std::vector<char>> anc(L, std::vector<char>(L, 0));
-  for (int i = 0; i < L; ++i)
-    for (int q : pred[i]) {
-      if (q >= i) report("edge against the launch order", q, i, 0);
-      anc[i][q] = 1;
-      for (int k = 0; k < L; ++k)
-        if (anc[q][k]) anc[i][k] = 1;
-    }
-  auto ordered = [&](int a, int b) { return a == b || anc[a][b] || anc[b][a]; };
-  // accesses: (launch, write?) per trace line, output region and scratch element range
-  std::map<long long, std::vector<std::pair<int, bool>>> trace, outreg;
-  std::vector<std::tuple<long long, long long, int>> scratch;
-  for (int i = 0; i < L; ++i) {
-    const Front& f = per.fronts[i];
-    for (int j = f.item_begin; j < f.item_begin + f.item_count; ++j) {
-      const DevItem& it = per.items[j];
-      const DevCell& c = cells[it.cell];
-      for (int q = 0; q < it.slot_count; ++q) {
-        const DevSlot& s = per.slots[it.slot_begin + q];
-        for (long long r : {s.in_lr0, s.in_lr1, s.in_ud0, s.in_ud1})
-          if (r >= 0) trace[r].push_back({i, false});
-        for (int l = 0; l < s.n_lr; ++l) trace[s.lr_out[l]].push_back({i, true});
-        for (int l = 0; l < s.n_ud; ++l) trace[s.ud_out[l]].push_back({i, true});
+      forked = true;
+      const int prev = last_of_lane[f.lane] >= 0 ? last_of_lane[f.lane] : last_stage1;
+      if (prev >= 0) u.pred.push_back(prev);
+      if (f.stage == 2) stage2_launch[{f.lane, f.step}] = id;
+      if (f.stage == 3) {
+        const int w = f.lane - 4, t = std::min(f.step + 1, N - 1);
+        for (int src : {kLaneProducerLR[w], kLaneProducerUD[w]}) {
+          auto it = stage2_launch.find({src, t});
+          if (it == stage2_launch.end()) report("missing producer launch", i, src, t);
+          else u.pred.push_back(it->second);
+        }
       }
-      for (int g = 0; g < it.group_count; ++g) {
-        const DevGroup& G = per.groups[it.group_begin + g];
-        if (G.out_off >= 0) outreg[G.out_off + it.cell].push_back({i, true});   // owned sets of cells are disjoint
-      }
-      const long long len = (long long)(c.nx + 1) * front_rpad(it.slot_count) * c.ny;
-      scratch.emplace_back(it.scratch_off, it.scratch_off + len, i);
+      last_of_lane[f.lane] = id;
+      units.push_back(u);
     }
   }
-  for (auto* acc : {&trace, &outreg})
-    for (const auto& kv : *acc) {
-      const auto& v = kv.second;
-      for (size_t a = 0; a < v.size(); ++a)
-        for (size_t b = a + 1; b < v.size(); ++b)
-          if ((v[a].second || v[b].second) && !ordered(v[a].first, v[b].first))
-            report(acc == &trace ? "unordered trace-line access" : "unordered output write", v[a].first,
-                   v[b].first, kv.first);
+  check_races(per, cells, units, report);
+  const int L = (int)units.size();
+
+  // 4. one launch per step with the per-shift streams of a captured apply: a
+  // front whose items each belong to one shifted decomposition runs as one
+  // launch per shift, shift s on stream s (shift 0 on the main stream), the
+  // side streams forked from the main stream before the first such front; a
+  // front with an item that mixes shifts joins every stream and runs alone on
+  // the main stream
+  std::vector<Unit> sunits;
+  {
+    std::vector<int> last(4, -1);          // last unit on each stream
+    std::vector<std::vector<int>> pending(4);
+    bool forked = false;
+    auto add = [&](int s, Unit u) {
+      if (last[s] >= 0) u.pred.push_back(last[s]);
+      for (int q : pending[s]) u.pred.push_back(q);
+      pending[s].clear();
+      last[s] = (int)sunits.size();
+      sunits.push_back(u);
+    };
+    for (int i = 0; i < (int)one.fronts.size(); ++i) {
+      const Front& f = one.fronts[i];
+      if (f.item_count <= 0) continue;
+      if (f.mixed) {
+        if (forked) {                      // join: the main stream waits for every side stream
+          for (int s = 1; s < 4; ++s)
+            if (last[s] >= 0) pending[0].push_back(last[s]);
+          forked = false;
+        }
+        add(0, Unit{i, f.item_begin, f.item_begin + f.item_count, {}});
+        continue;
+      }
+      if (!forked) {                       // fork: the side streams wait for the main stream
+        for (int s = 1; s < 4; ++s)
+          if (last[0] >= 0) pending[s].push_back(last[0]);
+        forked = true;
+      }
+      for (int sh = 0; sh < 4; ++sh)
+        if (f.sh_begin[sh + 1] > f.sh_begin[sh])
+          add(sh, Unit{i, f.item_begin + f.sh_begin[sh], f.item_begin + f.sh_begin[sh + 1], {}});
     }
-  std::sort(scratch.begin(), scratch.end());
-  for (size_t a = 0; a < scratch.size(); ++a)
-    for (size_t b = a + 1; b < scratch.size() && std::get<0>(scratch[b]) < std::get<1>(scratch[a]); ++b)
-      if (!ordered(std::get<2>(scratch[a]), std::get<2>(scratch[b])))
-        report("unordered scratch overlap", std::get<2>(scratch[a]), std::get<2>(scratch[b]),
-               std::get<0>(scratch[b]));
+  }
+  check_races(one, cells, sunits, report);
   if (bad) return 1;
-  std::printf("ok launches=%d steps=%d\n", L, (int)one.fronts.size());
+  std::printf("ok launches=%d steps=%d shift_launches=%d\n", L, (int)one.fronts.size(), (int)sunits.size());
   return 0;
 }
