@@ -64,6 +64,23 @@ def test_one_cell_precond_is_exact_inverse():
     assert np.linalg.norm(A @ z - v) <= 1e-12 * np.linalg.norm(v)
 
 
+@pytest.mark.parametrize("N,medium", [(3, "lens"), (4, "layered")])
+def test_precond_is_linear(N, medium):
+    """applyPrecond is a linear operator (sums of exact local solves of windows,
+    equivalent sources and traces that depend linearly on the input), as GMRES
+    requires: M(a x + b y) = a M x + b M y to rounding."""
+    _, _, P = _problem(N, medium=medium)
+    P.dd.factorize()
+    rng = np.random.default_rng(5)
+    n2 = P.n_dof ** 2
+    x = rng.standard_normal(n2) + 1j * rng.standard_normal(n2)
+    y = rng.standard_normal(n2) + 1j * rng.standard_normal(n2)
+    a, b = 0.7 - 0.2j, -1.3 + 0.4j
+    z = P.apply_precond_global(a * x + b * y)
+    w = a * P.apply_precond_global(x) + b * P.apply_precond_global(y)
+    assert np.linalg.norm(z - w) <= 1e-12 * np.linalg.norm(z)
+
+
 def test_shift_conversions_are_identity_on_global_vectors():
     _, _, P = _problem(3)
     rng = np.random.default_rng(3)
