@@ -1,8 +1,11 @@
 // Checks the sweep schedule of the library on the CPU (compiled with the
 // library's csrc/geometry.cpp, no GPU needed).
 //
-//   schedule_probe N m p nrhs
+//   schedule_probe N m p nrhs [slots]
 //
+// (slots: 4, 8 or 16 right-hand-side slots per item imposed on every launch,
+// as the tuner's candidates and LSW_FRONT_SHAPE impose them; default: the
+// cost model's choice)
 // Builds the one-launch-per-step schedule and the per-sweep schedule of an
 // N x N checkerboard of m-element cells with p PML elements, then checks:
 //  1. both schedules hold the same cell solves: per (stage, step, cell) the
@@ -56,8 +59,10 @@ struct Built {
   std::vector<DevGroup> groups;
 };
 
-static Built build(const std::vector<DevCell>& cells, int N, int nrhs, bool lanes, long long LP, long long n2) {
+static Built build(const std::vector<DevCell>& cells, int N, int nrhs, bool lanes, long long LP, long long n2,
+                   int slots) {
   FrontPlan plan;
+  if (slots > 0) plan.forced_r.assign(16 * (size_t)N + 16, slots);
   plan.max_clusters[1] = 76; plan.max_clusters[2] = 38; plan.max_clusters[4] = 19;
   for (int r = 1; r <= 16; ++r) plan.fit_mask[r] = (1 << 1) | (1 << 2) | (1 << 4);
   plan.lanes = lanes;
@@ -148,10 +153,11 @@ static void check_races(const Built& b, const std::vector<DevCell>& cells, const
 }
 
 int main(int argc, char** argv) {
-  if (argc != 5) {
-    std::fprintf(stderr, "usage: schedule_probe N m p nrhs\n");
+  if (argc != 5 && argc != 6) {
+    std::fprintf(stderr, "usage: schedule_probe N m p nrhs [slots]\n");
     return 2;
   }
+  const int slots = argc == 6 ? std::atoi(argv[5]) : 0;
   const int N = std::atoi(argv[1]), m = std::atoi(argv[2]), p = std::atoi(argv[3]), nrhs = std::atoi(argv[4]);
   const std::vector<DevCell> cells = make_cells(N, m, p);
   int max_n = 0;
@@ -159,8 +165,8 @@ int main(int argc, char** argv) {
   const long long LP = ((max_n + 7) / 8) * 8;
   const long long n_dof = (long long)N * m + N - 1 + 2 * p - 1;
   const long long n2 = n_dof * n_dof;
-  const Built one = build(cells, N, nrhs, false, LP, n2);
-  const Built per = build(cells, N, nrhs, true, LP, n2);
+  const Built one = build(cells, N, nrhs, false, LP, n2, slots);
+  const Built per = build(cells, N, nrhs, true, LP, n2, slots);
   int bad = 0;
   auto report = [&](const char* what, long long a, long long b, long long key) {
     if (bad < 40) std::printf("%s: launches %lld and %lld, key %lld\n", what, a, b, key);

@@ -54,3 +54,14 @@ def test_concurrent_launches_have_no_race(probe, N, m, p, nrhs):
     # stage 1, then four launches per stage-2 column and per stage-3 anti-diagonal
     assert steps == 1 + (N - 1) + (2 * N - 3)
     assert launches == 1 + 4 * (N - 1) + 4 * (2 * N - 3)
+
+
+@pytest.mark.parametrize("slots", [4, 8, 16])
+@pytest.mark.parametrize("N,m,p,nrhs", [(3, 12, 5, 1), (4, 16, 6, 2), (5, 7, 2, 8), (8, 128, 16, 16)])
+def test_no_race_with_imposed_item_sizes(probe, N, m, p, nrhs, slots):
+    """The same checks with every launch's items cut to 4, 8 or 16 slots (the
+    tuner's candidates, LSW_FRONT_SHAPE): the items of a cell and their
+    scratch change, the absence of races must not."""
+    r = subprocess.run([str(probe), str(N), str(m), str(p), str(nrhs), str(slots)], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
